@@ -1,0 +1,340 @@
+"""Benchmark of the PPSieve hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload (BASELINE configuration 2, "large-n Proth"): odd k in [1201, 9999],
+n in [2,000,000, 3,000,000), primes p in [4.2e13, 4.2e13 + 1e11).  One step is
+one pass of the hot path over one batch: the device sieve of the next 2^31-wide
+slice of that p range (about 6.8e7 primes), the walk of every prime over the
+whole n range, and the output filter.  Step i takes slice i, so the timed steps
+cover K consecutive slices of the configuration's range (47 slices make the whole
+range).  Inputs are generated on the device (the slice's primes are 1.1 GB,
+larger than the 129 MB L2, so no flush is needed between steps).
+
+value  = primes fully walked per second (whole job, all ranks).
+e2e    = the same metric through the drop-in C-ABI call with HOST buffers:
+         pps_check_primes() given the slice's primes in pinned host memory
+         (H2D copy inside the timed region) and returning the factor list to the
+         host (D2H inside the timed region) -- what the reference's check_ns /
+         get_factors_found boundary carries.
+roofline: the walk kernel is bound by the 32-bit integer multiply pipe; its
+         algorithmic work is 3 multiplies per walk step (one 32 n-values advance
+         of one prime); the peak is the multiply-pipe throughput measured in this
+         run by pps_measure_imad_peak on the same multiply mix.
+--impl reference: the reference's CPU algorithm (the committed C restatement in
+         oracle/, the reference's own build is not available on the GPU host) on
+         all host cores, one bounded sample of the same workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "psieve-cuda_gb300"))
+
+METRIC = "primes/sec & n-steps/sec, k<10^4 n 2M–3M; batched vs plain GPU; serve p50/p99"
+C2 = dict(pmin=42 * 10**12, pmax=42 * 10**12 + 10**11, kmin=1201, kmax=9999, nmin=2000000,
+          nmax=3000000)
+SPAN = 1 << 31
+WORKLOAD = ("config 2 large-n Proth: p in [4.2e13, 4.2e13+1e11), odd k in [1201, 9999], "
+            "n in [2e6, 3e6); one step = one 2^31-wide p slice")
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _traffic_from_profile() -> float | None:
+    f = ROOT / "profiles" / "walk_c2_ncu.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_step_of_one_prime:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def _measured_peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return json.loads(f.read_text())
+    except Exception:
+        return {}
+
+
+def cpu_sample(seconds_target: float = 10.0, nthreads: int | None = None) -> dict:
+    """Time the CPU restatement of the reference path on a bounded sample of the
+    workload (a p sub-range at the start of the configuration's range)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    nthreads = nthreads or oracle.threads()
+    width = 2 * 10**6
+    while True:
+        spec = dict(C2, pmax=C2["pmin"] + width)
+        p = oracle.normalize(**spec)
+        t0 = time.perf_counter()
+        _, count, _ = oracle.run(p, nthreads)
+        dt = time.perf_counter() - t0
+        if dt >= seconds_target * 0.5 or width >= 10**9:
+            break
+        width = int(width * min(8.0, max(1.5, seconds_target / max(dt, 1e-3))))
+    steps = (C2["nmax"] - C2["nmin"] + p.nstep - 1) // p.nstep
+    return {"value": count / dt, "unit": "primes/s", "cores": nthreads, "kind": "port",
+            "sample": f"p in [4.2e13, 4.2e13+{width}) = {count} primes, full n range, "
+                      f"{dt:.2f} s on {nthreads} threads",
+            "n_steps_per_sec": count * steps / dt, "seconds": dt, "primes": count}
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    per_step = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(seconds_target=args.ref_seconds)
+        if i >= args.warmup:
+            per_step.append(r)
+    value = statistics.median(r["value"] for r in per_step)
+    ms = statistics.median(r["seconds"] for r in per_step) * 1e3
+    last = per_step[-1]
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "primes/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (deterministic p range of the configuration)",
+            "config": {"workload": WORKLOAD, "sample": last["sample"]},
+            "cpu_baseline": {"value": value, "unit": "primes/s", "cores": last["cores"],
+                             "kind": "port", "sample": last["sample"]},
+            "e2e": {"value": value, "unit": "primes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "n_steps_per_sec": statistics.median(r["n_steps_per_sec"] for r in per_step)}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import ppsgpu
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    lib = ppsgpu.load()
+    eng = ppsgpu.Engine(local)
+    eng.set_batch_span(SPAN)
+
+    def slice_params(i: int):
+        lo = C2["pmin"] + i * SPAN
+        hi = min(C2["pmax"], lo + SPAN)
+        return ppsgpu.normalize(**dict(C2, pmin=lo, pmax=hi))
+
+    total_slices = (C2["pmax"] - C2["pmin"] + SPAN - 1) // SPAN
+    my_slices = [s for s in range(total_slices) if s % ws == rank]
+    need = args.warmup + args.steps
+    seq = [my_slices[i % len(my_slices)] for i in range(need)]
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if ws == 1:
+            return x
+        t = torch.tensor([x], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x: float) -> float:
+        if ws == 1:
+            return x
+        t = torch.tensor([x], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t)
+        return float(t.item())
+
+    # ---- device-resident path (value)
+    for i in range(args.warmup):
+        eng.run_job(slice_params(seq[i]))
+    barrier()
+    launches0 = eng.launches
+    stats = []
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.warmup, need):
+            _, st = eng.run_job(slice_params(seq[i]))
+            stats.append(st)
+        barrier()
+        elapsed = time.perf_counter() - t0
+    launches = eng.launches - launches0
+    primes = sum(s.primes for s in stats)
+    steps_done = sum(s.steps for s in stats)
+    walk_ms = sum(s.walk_ms for s in stats)
+    sieve_ms = sum(s.sieve_ms for s in stats)
+    elapsed = max_over_ranks(elapsed)
+    value = sum_over_ranks(primes) / elapsed
+    nsteps_rate = sum_over_ranks(steps_done) / elapsed
+
+    # ---- end-to-end through the host-buffer C ABI (e2e)
+    e2e = None
+    if not args.no_e2e:
+        host_sets = []
+        for i in range(need):
+            jp = slice_params(seq[i])
+            pr, n, _ = eng.sieve_range(jp.pmin, jp.pmax, jp.qmax, want_primes=True)
+            pin = torch.empty(n, dtype=torch.int64, pin_memory=True)
+            pin.numpy().view(np.uint64)[:] = pr
+            host_sets.append((jp, pin))
+        for i in range(args.warmup):
+            jp, pin = host_sets[i]
+            eng.check_primes(jp, pin.numpy().view(np.uint64))
+        barrier()
+        h2d = d2h = 0
+        e_primes = 0
+        t0 = time.perf_counter()
+        for i in range(args.warmup, need):
+            jp, pin = host_sets[i]
+            fac, st = eng.check_primes(jp, pin.numpy().view(np.uint64))
+            h2d += pin.numel() * 8
+            d2h += 8 + fac.nbytes
+            e_primes += st.primes
+        barrier()
+        e_el = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": sum_over_ranks(e_primes) / e_el, "unit": "primes/s",
+               "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
+               "path": "pps_check_primes (host primes in pinned memory -> factors to host)"}
+        del host_sets
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline of the walk kernel
+    peak_mults = eng.imad_peak()
+    mults = 3.0 * steps_done
+    achieved = mults / (walk_ms * 1e-3)
+    traffic = _traffic_from_profile()
+    peaks = _measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    sieve_gbs = 16.0 * primes / (sieve_ms * 1e-3) / 1e9 if sieve_ms > 0 else None
+    launches_walk = len(stats)
+    roofline = {"bound": "imad", "achieved": achieved / 1e9, "peak": peak_mults / 1e9,
+                "unit": "Gmul/s", "frac": achieved / peak_mults,
+                "traffic": (traffic * steps_done / launches_walk) if traffic else None,
+                "kernel": "k_walk", "peak_source": "measured in this run (pps_measure_imad_peak)",
+                "work_per_unit": "3 multiplies per walk step (one prime advanced by 32 n)",
+                "sieve": {"bound": "hbm", "achieved": sieve_gbs, "peak": hbm, "unit": "GB/s",
+                          "frac": (sieve_gbs / hbm) if (sieve_gbs and hbm) else None,
+                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                          "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
+    cpu = None if args.no_cpu else cpu_sample(args.ref_seconds)
+    line = {"metric": METRIC, "value": value, "unit": "primes/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (deterministic p range of the configuration, primes made on device)",
+            "config": {"workload": WORKLOAD, "slice_span": SPAN, "slices": seq[args.warmup:],
+                       "primes_per_step": primes / args.steps,
+                       "l2": "inputs larger than L2 (1.1 GB of primes per step), no flush",
+                       "variant": stats[-1].variant if stats else None},
+            "n_steps_per_sec": nsteps_rate, "gpu_launches": launches,
+            "phase_ms": {"sieve": sieve_ms, "walk": walk_ms,
+                         "filter": sum(s.filter_ms for s in stats)},
+            "factors": sum(s.factors for s in stats),
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/* ppsgpu.h -- C ABI of the GB300 PPSieve library (libppsgpu.so).
+
+   The path: for every odd prime p in [pmin, pmax) walk k = -/+2^-n (mod p) over
+   n in [nmin, nmax) and report every p | k*2^n+c (c = +1 Proth, -1 Riesel) with
+   k in [kmin, kmax], k == koffset (mod kstep), k*2^n+c free of odd prime factors
+   below 32768.  Everything runs on one GPU: a segmented sieve makes the primes,
+   a walk kernel finds candidates, a filter kernel applies the output rule.
+
+   Plain C types only; no CUDA or torch types cross this boundary.  All calls
+   return PPS_OK (0) or a negative error code and never exit the process.
+
+   Reference interfaces this library replaces (file:line in Ken-g6/PSieve-CUDA):
+     - the GPU C ABI pps/appcu.h:27-37 (cuda_init, cuda_app_init, check_ns,
+       get_factors_found, cuda_finalize, ld_nstep/ld_bbits/ld_r0): declared in
+       include/appcu_compat.h and exported by libppsgpu_appcu.so;
+     - the parameter rules of pps/app.c:649-712 and pps/appcu.cu:155-209:
+       pps_normalize below;
+     - check_ns + get_factors_found + the CPU re-walk pps/app.c:1037-1219 and
+       the filter pps/app.c:159-186: pps_check_primes / pps_run_job below,
+       which return exact (p, k, n, c) instead of per-subsection flags;
+     - the host prime generator sieve.c:168-1314 feeding main.c:750-777:
+       pps_sieve_range / the sieve inside pps_run_job.
+*/
+#ifndef PPSGPU_H
+#define PPSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The first four match pps/app.h:64-71. */
+#define PPS_OK                         0
+#define PPS_ERR_INVALID_PARAM       (-178)
+#define PPS_ERR_INSUFFICIENT_RESOURCE (-198)
+#define PPS_ERR_NOT_IMPLEMENTED     (-150)
+#define PPS_ERR_FOPEN               (-108)
+#define PPS_ERR_CUDA                (-300) /* a CUDA runtime call failed */
+#define PPS_ERR_NO_DEVICE           (-301) /* no usable GPU */
+#define PPS_ERR_OVERFLOW            (-302) /* caller's output buffer too small */
+#define PPS_ERR_TIMEOUT             (-303) /* a bounded device wait expired */
+#define PPS_ERR_BUSY                (-304) /* server queue / memory budget full */
+#define PPS_ERR_NOT_FOUND           (-305) /* unknown job id */
+#define PPS_ERR_CANCELLED           (-306)
+
+/* A job as the user states it; zero means "not given" exactly as in the
+   reference options (-p -P -k -K -n -N -R -M -s -Q). */
+typedef struct {
+  uint64_t pmin, pmax;
+  uint64_t kmin, kmax;
+  uint32_t nmin, nmax;
+  int32_t  sign;      /* +1 Proth (default when 0), -1 Riesel (-R) */
+  uint32_t kstep;     /* -M, default 2 */
+  uint32_t koffset;   /* -s, default 1 */
+  uint32_t qmax;      /* -Q, default sqrt(pmax) */
+} pps_job_spec;
+
+/* A job after the reference's normalisation (pps_normalize). */
+typedef struct {
+  uint64_t pmin, pmax;   /* primes pmin <= p < pmax */
+  uint64_t kmin, kmax;   /* rounded to kstep*b+koffset (pps/app.c:705-708) */
+  uint32_t nmin, nmax;   /* n in [nmin, nmax) */
+  int32_t  sign;
+  uint32_t kstep, koffset;
+  uint32_t qmax;         /* sieving primes q <= qmax */
+  uint32_t nstep;        /* the reference's ld_nstep after pps/appcu.cu:158-186 */
+  uint32_t step;         /* n values per device walk step: min(nstep, 32) */
+} pps_job_params;
+
+/* One reported factor: p | k*2^n+c. */
+typedef struct {
+  uint64_t p;
+  uint64_t k;
+  uint32_t n;
+  int32_t  c;
+} pps_factor;
+
+/* One raw candidate before the output filter (k in range, n < nmax). */
+typedef struct {
+  uint64_t p;
+  uint64_t k;
+  uint32_t n;
+  uint32_t idx;   /* index of p in the caller's prime list, or job slot */
+} pps_hit;
+
+typedef struct {
+  uint64_t primes;      /* primes walked */
+  uint64_t prime_sum;   /* wrapping 64-bit sum of those primes (main.c:1232) */
+  uint64_t raw_hits;    /* candidates before the output filter */
+  uint64_t factors;     /* lines reported */
+  uint64_t steps;       /* walk steps executed (primes x ceil((nmax-nmin)/step)) */
+  uint32_t batches;     /* device batches used */
+  uint32_t variant;     /* walk kernel variant used */
+  double   sieve_ms, walk_ms, filter_ms, total_ms;  /* device time per phase */
+} pps_job_stats;
+
+typedef struct pps_engine pps_engine;
+
+/* Last error message of the calling thread ("" if none). */
+const char *pps_last_error(void);
+
+/* Library version string. */
+const char *pps_version(void);
+
+/* Apply the reference's option rules (main.c:916-931, main.c:971-972,
+   pps/app.c:657-712, pps/appcu.cu:158-204, pps/appcu.cu:236). */
+int pps_normalize(const pps_job_spec *in, pps_job_params *out);
+
+/* Engine: one per GPU and host thread; owns streams, device buffers and the
+   tuned kernel choice.  device < 0 picks device 0. */
+int pps_engine_create(int device, pps_engine **out);
+void pps_engine_destroy(pps_engine *e);
+
+/* Device memory held by the engine, in bytes. */
+uint64_t pps_engine_device_bytes(const pps_engine *e);
+
+/* Batch width of the p-range per device sieve batch (default 2^31).  Smaller
+   batches lower memory; results do not depend on it. */
+int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
+
+/* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
+#define PPS_NUM_VARIANTS 6
+int pps_engine_set_variant(pps_engine *e, int variant);
+
+/* Whole job: device sieve of [pmin,pmax), walk, filter.  Factors are sorted by
+   (p, k, n); *nout is the total found (may exceed cap -> PPS_ERR_OVERFLOW, with
+   the first cap entries written). */
+int pps_run_job(pps_engine *e, const pps_job_params *jp, pps_factor *out,
+                size_t cap, size_t *nout, pps_job_stats *st);
+
+/* Walk a caller-supplied list of primes held in HOST memory (copied to the
+   device inside the call).  Same output rule and order as pps_run_job. */
+int pps_check_primes(pps_engine *e, const pps_job_params *jp, const uint64_t *P,
+                     size_t np, pps_factor *out, size_t cap, size_t *nout,
+                     pps_job_stats *st);
+
+/* Same walk, returning the raw candidates (before the output filter), with
+   pps_hit.idx = index into P.  Used by the pps/appcu.h compatibility layer to
+   build per-subsection flags. Sorted by (idx, n). */
+int pps_check_primes_raw(pps_engine *e, const pps_job_params *jp, const uint64_t *P,
+                         size_t np, pps_hit *out, size_t cap, size_t *nout);
+
+/* Walk primes already resident in device memory (d_P: np uint64 values).
+   Factors are written to host memory. */
+int pps_check_primes_device(pps_engine *e, const pps_job_params *jp,
+                            const uint64_t *d_P, size_t np, pps_factor *out,
+                            size_t cap, size_t *nout, pps_job_stats *st);
+
+/* Device sieve of odd primes in [lo, hi) with sieving primes q <= qmax
+   (0 = floor(sqrt(hi-1)) rule of main.c:971-972).  Writes up to cap primes to
+   out (host, may be NULL), returns count and wrapping sum. */
+int pps_sieve_range(pps_engine *e, uint64_t lo, uint64_t hi, uint32_t qmax,
+                    uint64_t *out, size_t cap, size_t *count, uint64_t *sum);
+
+/* Measured throughput of the device's 32-bit multiply pipe on the walk's own
+   multiply mix (one lo, one hi, one wide multiply), in multiplies per second.
+   The roofline denominator for the walk kernel. */
+int pps_measure_imad_peak(pps_engine *e, double *mults_per_sec);
+
+/* Number of the engine's own kernels launched so far. */
+uint64_t pps_engine_launches(const pps_engine *e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,172 @@
+"""Python binding of the CPU oracle (oracle/_build/libppsoracle.so).
+
+ORACLE / TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke()
+as the checker and by bench.py's CPU-baseline leg.  The shipped library never
+imports it.  The C code it wraps restates the reference's CPU path; see
+pps_oracle.h for the file:line map.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libppsoracle.so"
+CLI = HERE / "_build" / "pps_oracle"
+REF_DIR = HERE / "_ref"
+
+FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u8"), ("n", "<u4"), ("c", "<i4")])
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("pmin", ctypes.c_uint64), ("pmax", ctypes.c_uint64),
+                ("kmin", ctypes.c_uint64), ("kmax", ctypes.c_uint64),
+                ("nmin", ctypes.c_uint32), ("nmax", ctypes.c_uint32),
+                ("c", ctypes.c_int32), ("kstep", ctypes.c_uint32),
+                ("koffset", ctypes.c_uint32), ("qmax", ctypes.c_uint32),
+                ("nstep", ctypes.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def build() -> None:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        lib = ctypes.CDLL(str(LIB))
+        P = ctypes.POINTER
+        lib.ppo_normalize.restype = ctypes.c_int
+        lib.ppo_normalize.argtypes = [P(Params), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                      ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.c_uint32]
+        lib.ppo_run.restype = ctypes.c_long
+        lib.ppo_run.argtypes = [P(Params), ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
+                                P(ctypes.c_uint64), P(ctypes.c_uint64)]
+        lib.ppo_walk_list.restype = ctypes.c_long
+        lib.ppo_walk_list.argtypes = [P(Params), P(ctypes.c_uint64), ctypes.c_size_t, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_size_t]
+        lib.ppo_small_factor.restype = ctypes.c_uint32
+        lib.ppo_small_factor.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32]
+        lib.ppo_small_factor_from.restype = ctypes.c_uint32
+        lib.ppo_small_factor_from.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32,
+                                              ctypes.c_uint32]
+        lib.ppo_test_factor.restype = ctypes.c_int
+        lib.ppo_test_factor.argtypes = [P(Params), ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32]
+        lib.ppo_is_prime.restype = ctypes.c_int
+        lib.ppo_is_prime.argtypes = [ctypes.c_uint64]
+        lib.ppo_kpow_mod.restype = ctypes.c_uint64
+        lib.ppo_kpow_mod.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64]
+        lib.ppo_sieve_range.restype = ctypes.c_size_t
+        lib.ppo_sieve_range.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                        P(ctypes.c_uint64), ctypes.c_size_t]
+        _lib = lib
+    return _lib
+
+
+class OracleError(ValueError):
+    pass
+
+
+def normalize(pmin=0, pmax=0, kmin=0, kmax=0, nmin=0, nmax=0, sign=1, kstep=0, koffset=0,
+              qmax=0) -> Params:
+    lib = load()
+    p = Params()
+    rc = lib.ppo_normalize(ctypes.byref(p), pmin, pmax, kmin, kmax, nmin, nmax, sign, kstep,
+                           koffset, qmax)
+    if rc:
+        raise OracleError(rc)
+    return p
+
+
+def threads() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+def run(params: Params, nthreads: int | None = None, cap: int = 1 << 16):
+    """Whole range on the CPU: (factors ndarray sorted by (p,k,n), count, sum)."""
+    lib = load()
+    while True:
+        out = np.zeros(cap, dtype=FACTOR_DTYPE)
+        cnt, s = ctypes.c_uint64(), ctypes.c_uint64()
+        n = lib.ppo_run(ctypes.byref(params), nthreads or threads(),
+                        out.ctypes.data_as(ctypes.c_void_p), cap, ctypes.byref(cnt),
+                        ctypes.byref(s))
+        if n > cap:
+            cap = n
+            continue
+        return out[:n].copy(), cnt.value, s.value
+
+
+def walk_list(params: Params, primes, nthreads: int | None = None, cap: int = 1 << 16):
+    lib = load()
+    P = np.ascontiguousarray(primes, dtype=np.uint64)
+    while True:
+        out = np.zeros(cap, dtype=FACTOR_DTYPE)
+        n = lib.ppo_walk_list(ctypes.byref(params), P.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                              len(P), nthreads or threads(), out.ctypes.data_as(ctypes.c_void_p), cap)
+        if n > cap:
+            cap = n
+            continue
+        return out[:n].copy()
+
+
+def sieve_range(lo: int, hi: int, qmax: int) -> np.ndarray:
+    lib = load()
+    n = lib.ppo_sieve_range(lo, hi, qmax, None, 0)
+    out = np.zeros(max(n, 1), dtype=np.uint64)
+    lib.ppo_sieve_range(lo, hi, qmax, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n)
+    return out[:n]
+
+
+def small_factor(k: int, n: int, c: int, qmin: int = 3) -> int:
+    return int(load().ppo_small_factor_from(k, n, c, qmin))
+
+
+def test_factor(params: Params, k: int, n: int, c: int) -> bool:
+    return bool(load().ppo_test_factor(ctypes.byref(params), k, n, c))
+
+
+def is_prime(x: int) -> bool:
+    return bool(load().ppo_is_prime(x))
+
+
+def kpow_mod(k: int, n: int, c: int, p: int) -> int:
+    return int(load().ppo_kpow_mod(k, n, c, p))
+
+
+def verify_line(p: int, k: int, n: int, c: int) -> bool:
+    """Per-line check kept for every run: p prime and p | k*2^n+c."""
+    return is_prime(p) and kpow_mod(k, n, c, p) == 0
+
+
+def tuples(arr) -> list[tuple[int, int, int, int]]:
+    return [(int(r["p"]), int(r["k"]), int(r["n"]), int(r["c"])) for r in arr]
+
+
+def format_line(p: int, k: int, n: int, c: int) -> str:
+    return f"{p} | {k}*2^{n}{c:+d}"
+
+
+def parse_line(line: str) -> tuple[int, int, int, int]:
+    left, right = line.split("|")
+    p = int(left.strip())
+    kpart, rest = right.strip().split("*2^")
+    if "+" in rest:
+        n, c = rest.split("+")
+        return p, int(kpart), int(n), int(c)
+    n, c = rest.split("-")
+    return p, int(kpart), int(n), -int(c)

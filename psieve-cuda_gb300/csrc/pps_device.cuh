@@ -1,0 +1,137 @@
+// pps_device.cuh -- device integer arithmetic for the PPSieve walk (sm_103a).
+//
+// Everything is exact 64-bit modular arithmetic built from 32-bit multiplies.
+// Conventions: p is an odd prime, 2^32 < p < 2^62; ps = -p^-1 mod 2^64.
+//
+// Reference counterparts (file:line in Ken-g6/PSieve-CUDA):
+//   neg_inv64      pps/appcu.cu:491-511 invmod2pow_ul (Newton lifting of p^-1)
+//   mont_mul       pps/appcu.cu:513-546 mulmod_REDC (R = 2^64 Montgomery product)
+//   inv_pow2       pps/appcu.cu:710-736 invpowmod_REDClr (2^-e mod p, left to right)
+//   step_*         pps/appcu.cu:591-707 shiftmod_REDC* (k <- k * 2^-s mod p)
+#pragma once
+#include <stdint.h>
+
+namespace pps {
+
+__device__ __forceinline__ uint32_t lo32(uint64_t x) { return (uint32_t)x; }
+__device__ __forceinline__ uint32_t hi32(uint64_t x) { return (uint32_t)(x >> 32); }
+__device__ __forceinline__ uint64_t mk64(uint32_t lo, uint32_t hi) {
+  return ((uint64_t)hi << 32) | lo;
+}
+
+// -p^-1 mod 2^64.  (3p) xor 2 inverts p modulo 2^5; each Newton step
+// x <- x(2 - p x) doubles the number of correct low bits: 5, 10, 20, 40 (so 32)
+// in 32-bit arithmetic, then one 64-bit step gives 64.
+__device__ __forceinline__ uint64_t neg_inv64(uint64_t p) {
+  const uint32_t p32 = (uint32_t)p;
+  uint32_t x = (3u * p32) ^ 2u;
+  x *= 2u - p32 * x;
+  x *= 2u - p32 * x;
+  x *= 2u - p32 * x;
+  uint64_t y = x;
+  y *= 2ull - p * y;
+  return 0ull - y;
+}
+
+// Montgomery product a*b*2^-64 mod p for a, b < p.  T = a*b < p^2, so
+// (T + m p) / 2^64 < p^2/2^64 + p < 2p and one conditional subtraction suffices.
+__device__ __forceinline__ uint64_t mont_mul(uint64_t a, uint64_t b, uint64_t p, uint64_t ps) {
+  const uint64_t tlo = a * b;
+  const uint64_t thi = __umul64hi(a, b);
+  const uint64_t m = tlo * ps;
+  const uint64_t r = thi + __umul64hi(m, p) + (tlo != 0ull ? 1ull : 0ull);
+  return r >= p ? r - p : r;
+}
+
+// x*2^-64 mod p (leaves Montgomery form).
+__device__ __forceinline__ uint64_t mont_out(uint64_t x, uint64_t p, uint64_t ps) {
+  const uint64_t m = x * ps;
+  const uint64_t r = __umul64hi(m, p) + (x != 0ull ? 1ull : 0ull);
+  return r >= p ? r - p : r;
+}
+
+// 2^-e mod p for e >= 32, p > 2^32.
+// Left to right over the bits of e.  The six leading bits t (32 <= t < 64) give
+// the Montgomery form of 2^-t directly as 2^(64-t) (< 2^32 < p, already
+// reduced); each further bit squares (doubling the exponent) and, for a 1 bit,
+// halves mod p (2^-1 factor).  Leaves Montgomery form at the end.
+__device__ __forceinline__ uint64_t inv_pow2(uint32_t e, uint64_t p, uint64_t ps) {
+  const int len = 32 - __clz(e);       // bit length, >= 6 because e >= 32
+  int b = len - 6;
+  uint64_t r = 1ull << (64 - (e >> b));
+  for (--b; b >= 0; --b) {
+    r = mont_mul(r, r, p, ps);
+    if ((e >> b) & 1u) r = (r & 1ull) ? ((r >> 1) + (p >> 1) + 1ull) : (r >> 1);
+  }
+  return mont_out(r, p, ps);
+}
+
+// ---------------------------------------------------------------- the walk step
+// K <- K * 2^-s mod p for K < p, 1 <= s <= 32, as (K + m p) / 2^s with
+// m = (-K p^-1) mod 2^s.  Because K < p (not K < p 2^s as in a full product
+// reduction), (K + m p)/2^s <= (p - 1 + (2^s - 1) p)/2^s < p: the result is
+// already reduced and no final subtraction is needed.
+//
+// With m' = m * 2^(32-s) = (Klo * pinv_s) mod 2^32, pinv_s = (ps mod 2^32) << (32-s):
+//   (K + m p)/2^s = (K >> s) + m' * phi + hi32(m' * plo) + [m' != 0]
+// (the low words of (K mod 2^s) 2^(32-s) and m' plo sum to 0 or 2^32).
+//
+// Three formulations of the same arithmetic; the autotuner times them.
+
+// Form 0: one lo multiply, one hi multiply, one wide multiply-add.
+template <bool S32>
+__device__ __forceinline__ void step_form0(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi,
+                                           uint32_t pinv_s, uint32_t s) {
+  const uint32_t m = klo * pinv_s;
+  uint64_t base;
+  if (S32) {
+    base = (uint64_t)khi;
+  } else {
+    base = mk64(__funnelshift_r(klo, khi, s), khi >> s);
+  }
+  const uint64_t r = base + __umulhi(m, plo) + (m != 0u ? 1u : 0u) + (uint64_t)m * phi;
+  klo = lo32(r);
+  khi = hi32(r);
+}
+
+// Form 1 (s = 32 only): 32-bit multiply-add carry chain over the 96-bit sum
+// K + m p, keeping words 1 and 2.
+__device__ __forceinline__ void step_chain32(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi,
+                                             uint32_t pinv) {
+  const uint32_t m = klo * pinv;
+  uint32_t w1, w2;
+  asm("{\n\t"
+      ".reg .u32 w0;\n\t"
+      "mad.lo.cc.u32  w0, %2, %3, %4;\n\t"   // w0 = lo(m plo) + klo  (== 0), carry
+      "madc.hi.cc.u32 %0, %2, %3, %5;\n\t"   // w1 = hi(m plo) + khi + carry
+      "madc.hi.u32    %1, %2, %6, 0;\n\t"    // w2 = hi(m phi) + carry
+      "mad.lo.cc.u32  %0, %2, %6, %0;\n\t"   // w1 += lo(m phi)
+      "addc.u32       %1, %1, 0;\n\t"        // w2 += carry
+      "}"
+      : "=r"(w1), "=r"(w2)
+      : "r"(m), "r"(plo), "r"(klo), "r"(khi), "r"(phi));
+  klo = w1;
+  khi = w2;
+}
+
+// Form 2: the low product m' plo + (K mod 2^s) 2^(32-s) as one wide
+// multiply-add whose high word is hi32(m' plo) + [m' != 0], then a second wide
+// multiply-add by phi.
+template <bool S32>
+__device__ __forceinline__ void step_form2(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi,
+                                           uint32_t pinv_s, uint32_t s) {
+  const uint32_t m = klo * pinv_s;
+  uint64_t x, base;
+  if (S32) {
+    x = (uint64_t)m * plo + klo;
+    base = (uint64_t)khi;
+  } else {
+    x = (uint64_t)m * plo + (klo << (32u - s));
+    base = mk64(__funnelshift_r(klo, khi, s), khi >> s);
+  }
+  const uint64_t r = (uint64_t)m * phi + (base + (x >> 32));
+  klo = lo32(r);
+  khi = hi32(r);
+}
+
+}  // namespace pps

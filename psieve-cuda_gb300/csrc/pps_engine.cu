@@ -1,0 +1,764 @@
+// pps_engine.cu -- host side of libppsgpu.so: the C ABI of include/ppsgpu.h.
+//
+// One engine = one GPU + one CUDA stream + device buffers that are grown on
+// demand and reused across calls.  A job is processed in p-range batches:
+//   device sieve (primes + Montgomery constants to HBM) -> walk kernel (raw
+//   hits appended to a device buffer) ; after the last batch the filter kernel
+//   applies the output rule and the survivors are copied to the caller.
+// Reference call stack this replaces (Ken-g6/PSieve-CUDA): main.c:736-783
+// (host sieve feeding batches) -> pps/app.c:1224-1250 -> pps/appcu.cu:1205-1308
+// (check_ns / get_factors_found) -> pps/app.c:1197-1219 (CPU re-walk) ->
+// pps/app.c:159-186 (filter) -> pps/app.c:124-148 (report).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "pps_internal.h"
+#include "ppsgpu.h"
+
+using namespace pps;
+
+// --------------------------------------------------------------- errors
+static thread_local char g_err[512];
+
+static int set_err(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+extern "C" const char* pps_last_error(void) { return g_err; }
+extern "C" const char* pps_version(void) { return "ppsgpu-0.1 (sm_103a)"; }
+
+#define CU(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return set_err(PPS_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),      \
+                     __FILE__, __LINE__);                                                \
+  } while (0)
+
+// ------------------------------------------------------------ normalize
+static int lg2u64(uint64_t v) {
+  int r = 0;
+  while (v >>= 1) r++;
+  return r;
+}
+
+extern "C" int pps_normalize(const pps_job_spec* in, pps_job_params* o) {
+  if (!in || !o) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  const uint64_t PMAX_MAX = 1ull << 62;  // main.h:43
+  memset(o, 0, sizeof *o);
+  uint64_t pmin = in->pmin, pmax = in->pmax, kmin = in->kmin, kmax = in->kmax;
+  uint32_t nmin = in->nmin, nmax = in->nmax, qmax = in->qmax;
+  uint32_t kstep = in->kstep ? in->kstep : 2u;    // pps/app.c:57
+  uint32_t koffset = in->koffset ? in->koffset : 1u;  // pps/app.c:58
+  int32_t sign = in->sign ? in->sign : 1;
+  if (sign != 1 && sign != -1) return set_err(PPS_ERR_INVALID_PARAM, "sign must be +1 or -1");
+  // main.c:916-931
+  if (pmin < 3) pmin = 3;
+  if (pmax > PMAX_MAX) pmax = PMAX_MAX;
+  if (pmin >= pmax) {
+    if (pmax == 0 && pmin < PMAX_MAX - 1000000000ull)
+      pmax = pmin + 1000000000ull;
+    else
+      return set_err(PPS_ERR_INVALID_PARAM, "pmax must be greater than pmin");
+  }
+  // main.c:971-972, sieve.c:98-110
+  if (qmax == 0) qmax = 1u << 31;
+  if ((uint64_t)qmax * qmax > pmax) qmax = (uint32_t)sqrt((double)pmax);
+  if (qmax < 61) qmax = 61;
+  // pps/app.c:657-700
+  if (kmin == 0 || kmax == 0)
+    return set_err(PPS_ERR_INVALID_PARAM, "Please specify an input file or all of kmin, kmax, and nmax");
+  if (kmin > kmax) return set_err(PPS_ERR_INVALID_PARAM, "kmin <= kmax is required");
+  if (kmax >= pmin) return set_err(PPS_ERR_INVALID_PARAM, "kmax < pmin is required");
+  if (kmax - kmin >= (3ull << 36)) return set_err(PPS_ERR_INVALID_PARAM, "kmax-kmin < 3*2^36 is required");
+  if (nmin == 0) nmin = (uint32_t)(2 * lg2u64(pmin) - lg2u64(kmax) - 1);
+  if (nmax == 0) nmax = nmin;
+  if (nmin > nmax) return set_err(PPS_ERR_INVALID_PARAM, "nmin <= nmax is required");
+  // pps/app.c:703-712
+  kmin = (kmin / kstep) * kstep + koffset;
+  kmax = (kmax / kstep) * kstep + koffset;
+  uint32_t nstep = 1;
+  while ((kmax << nstep) < pmin) nstep++;
+  // pps/appcu.cu:158-204
+  if (nstep > nmax - nmin + 1) nstep = nmax - nmin + 1;
+  if ((1ull << (64 - nstep)) > pmin)
+    return set_err(PPS_ERR_INVALID_PARAM, "pmin is not large enough (or nmax is close to nmin)");
+  if (nstep >= 32 && nstep < 48 && (1ull << 32) <= pmin) nstep = 32;
+  if (lg2u64(nmin) < 6) return set_err(PPS_ERR_INVALID_PARAM, "nmin too small at %u (must be at least 64)", nmin);
+  // pps/appcu.cu:236-239
+  if (pmin <= (1ull << 32)) return set_err(PPS_ERR_INVALID_PARAM, "PMin is too small, <= 2^32");
+  o->pmin = pmin;
+  o->pmax = pmax;
+  o->kmin = kmin;
+  o->kmax = kmax;
+  o->nmin = nmin;
+  o->nmax = nmax;
+  o->sign = sign;
+  o->kstep = kstep;
+  o->koffset = koffset;
+  o->qmax = qmax;
+  o->nstep = nstep;
+  o->step = nstep < 32 ? nstep : 32;
+  return PPS_OK;
+}
+
+// ---------------------------------------------------------------- engine
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  int ensure(size_t want) {
+    if (want <= n) return PPS_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    size_t grow = want + want / 8;
+    cudaError_t e = cudaMalloc(&p, grow * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "cudaMalloc(%zu bytes): %s",
+                     grow * sizeof(T), cudaGetErrorString(e));
+    }
+    n = grow;
+    return PPS_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+struct pps_engine {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[8] = {};
+  uint64_t batch_span = 1ull << 31;
+  int forced_variant = -1;
+  int tuned_variant[2] = {-1, -1};  // [step==32]
+  uint64_t launches = 0;
+
+  // sieving primes (ascending odd primes <= base_limit), u32
+  DevBuf<uint32_t> base_q;
+  uint32_t base_limit = 0;
+  uint32_t base_count = 0;
+  std::vector<uint32_t> host_seed;  // odd primes < SEG_BITS (host copy)
+  DevBuf<uint32_t> seed_q;
+
+  DevBuf<uint32_t> bitmap, seg_count, seg_off;
+  DevBuf<uint64_t> P, Pinv;
+  DevBuf<uint64_t> totals;  // [0] count, [1] sum
+  DevBuf<pps_hit> hits;
+  DevBuf<pps_factor> factors;
+  DevBuf<uint32_t> counters;  // [0] raw hits, [1] factors
+  DevBuf<uint16_t> small_q;
+  uint32_t nsmall = 0;
+  DevBuf<uint32_t> probe_sink;
+  uint64_t* h_pinned = nullptr;  // 16 words of pinned host scratch
+};
+
+static void free_engine(pps_engine* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  e->base_q.release();
+  e->seed_q.release();
+  e->bitmap.release();
+  e->seg_count.release();
+  e->seg_off.release();
+  e->P.release();
+  e->Pinv.release();
+  e->totals.release();
+  e->hits.release();
+  e->factors.release();
+  e->counters.release();
+  e->small_q.release();
+  e->probe_sink.release();
+  if (e->h_pinned) cudaFreeHost(e->h_pinned);
+  for (auto& v : e->ev)
+    if (v) cudaEventDestroy(v);
+  if (e->st) cudaStreamDestroy(e->st);
+  delete e;
+}
+
+extern "C" void pps_engine_destroy(pps_engine* e) { free_engine(e); }
+
+static std::vector<uint32_t> host_odd_primes(uint32_t limit) {
+  std::vector<uint8_t> comp(limit + 1, 0);
+  std::vector<uint32_t> r;
+  for (uint32_t i = 3; i <= limit; i += 2) {
+    if (comp[i]) continue;
+    r.push_back(i);
+    for (uint64_t j = (uint64_t)i * i; j <= limit; j += 2ull * i) comp[j] = 1;
+  }
+  return r;
+}
+
+extern "C" int pps_engine_create(int device, pps_engine** out) {
+  if (!out) return set_err(PPS_ERR_INVALID_PARAM, "null out");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_err(PPS_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (device < 0) device = 0;
+  if (device >= ndev) return set_err(PPS_ERR_NO_DEVICE, "device %d not present (%d devices)", device, ndev);
+  pps_engine* e = new pps_engine();
+  e->device = device;
+  int rc = PPS_OK;
+  do {
+    if (cudaSetDevice(device) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "cudaSetDevice failed"); break; }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "cudaGetDeviceProperties failed"); break; }
+    e->num_sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "stream"); break; }
+    for (auto& v : e->ev)
+      if (cudaEventCreate(&v) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "event"); break; }
+    if (rc) break;
+    if (cudaMallocHost(&e->h_pinned, 16 * sizeof(uint64_t)) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "pinned"); break; }
+    // odd primes 3..32749 for the output filter (pps/factor_proth.c:26-42 range)
+    std::vector<uint32_t> sp = host_odd_primes(32767);
+    std::vector<uint16_t> sp16(sp.begin(), sp.end());
+    e->nsmall = (uint32_t)sp16.size();
+    if ((rc = e->small_q.ensure(sp16.size()))) break;
+    if (cudaMemcpy(e->small_q.p, sp16.data(), sp16.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "copy"); break; }
+    e->host_seed = host_odd_primes(SEG_BITS - 1);
+    if ((rc = e->seed_q.ensure(e->host_seed.size()))) break;
+    if (cudaMemcpy(e->seed_q.p, e->host_seed.data(), e->host_seed.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "copy"); break; }
+    if ((rc = e->counters.ensure(8))) break;
+    if ((rc = e->totals.ensure(4))) break;
+  } while (0);
+  if (rc) {
+    free_engine(e);
+    return rc;
+  }
+  *out = e;
+  return PPS_OK;
+}
+
+extern "C" uint64_t pps_engine_device_bytes(const pps_engine* e) {
+  if (!e) return 0;
+  return e->base_q.bytes() + e->seed_q.bytes() + e->bitmap.bytes() + e->seg_count.bytes() +
+         e->seg_off.bytes() + e->P.bytes() + e->Pinv.bytes() + e->totals.bytes() + e->hits.bytes() +
+         e->factors.bytes() + e->counters.bytes() + e->small_q.bytes() + e->probe_sink.bytes();
+}
+
+extern "C" int pps_engine_set_batch_span(pps_engine* e, uint64_t span) {
+  if (!e || span < 2ull * SEG_BITS) return set_err(PPS_ERR_INVALID_PARAM, "batch span too small");
+  e->batch_span = span & ~1ull;
+  return PPS_OK;
+}
+
+extern "C" int pps_engine_set_variant(pps_engine* e, int v) {
+  if (!e || v < -1 || v >= PPS_NUM_VARIANTS) return set_err(PPS_ERR_INVALID_PARAM, "bad variant %d", v);
+  e->forced_variant = v;
+  return PPS_OK;
+}
+
+extern "C" uint64_t pps_engine_launches(const pps_engine* e) { return e ? e->launches : 0; }
+
+// ----------------------------------------------------------------- sieve
+static uint32_t isqrt64(uint64_t x) {
+  uint64_t r = (uint64_t)sqrt((double)x);
+  while (r * r > x) r--;
+  while ((r + 1) * (r + 1) <= x) r++;
+  return (uint32_t)r;
+}
+
+static int sieve_batch(pps_engine* e, uint64_t lo, uint64_t hi, const uint32_t* dq, uint32_t nq,
+                       uint32_t nq_tiny, uint32_t nq_seg, uint64_t* out64, uint64_t* pinv64,
+                       uint32_t* out32) {
+  SieveBatch b;
+  b.lo = lo | 1ull;
+  if (hi <= b.lo) return PPS_OK;
+  b.nbits = (hi - b.lo + 1) / 2;
+  b.nseg = (uint32_t)((b.nbits + SEG_BITS - 1) / SEG_BITS);
+  int rc;
+  if ((rc = e->bitmap.ensure((size_t)b.nseg * SEG_WORDS))) return rc;
+  if ((rc = e->seg_count.ensure(b.nseg))) return rc;
+  if ((rc = e->seg_off.ensure(b.nseg))) return rc;
+  b.q = dq;
+  b.nq = nq;
+  b.nq_tiny = nq_tiny;
+  b.nq_seg = nq_seg;
+  b.bitmap = e->bitmap.p;
+  b.seg_count = e->seg_count.p;
+  b.seg_off = e->seg_off.p;
+  b.d_total = e->totals.p;
+  CU(cudaMemsetAsync(e->totals.p, 0, 2 * sizeof(uint64_t), e->st));
+  e->launches += launch_sieve_batch(b, out64, pinv64, out32, e->st);
+  CU(cudaGetLastError());
+  return PPS_OK;
+}
+
+static uint32_t count_le(const std::vector<uint32_t>& v, uint32_t x) {
+  return (uint32_t)(std::upper_bound(v.begin(), v.end(), x) - v.begin());
+}
+
+struct BaseTable {
+  uint32_t nq, nq_tiny, nq_seg;
+};
+
+// Make sure the device holds all odd primes <= limit and fill the counts.
+// Returns 1 when the host-made seed table (odd primes < SEG_BITS) serves,
+// 0 when the device-made table base_q does, or a negative error.
+static int ensure_base(pps_engine* e, uint32_t limit, BaseTable* bt) {
+  if (limit < 3) limit = 3;
+  if (limit < SEG_BITS) {
+    // straight from the host seed list
+    uint32_t n = count_le(e->host_seed, limit);
+    bt->nq = n;
+    bt->nq_tiny = count_le(e->host_seed, TINY_Q_LIMIT - 1);
+    if (bt->nq_tiny > n) bt->nq_tiny = n;
+    bt->nq_seg = std::min(n, count_le(e->host_seed, SEG_BITS - 1));
+    return 1;
+  }
+  if (e->base_limit < limit) {
+    // odd primes in [3, limit] with seeds <= sqrt(limit) (all < 2^16)
+    const uint32_t root = isqrt64(limit);
+    const uint32_t ns = count_le(e->host_seed, root);
+    const uint32_t ns_tiny = std::min(ns, count_le(e->host_seed, TINY_Q_LIMIT - 1));
+    // capacity: pi(limit) < 1.26 limit / ln(limit)
+    const size_t cap = (size_t)(1.3 * limit / log((double)limit)) + 1024;
+    int rc;
+    if ((rc = e->base_q.ensure(cap))) return rc;
+    uint64_t filled = 0;
+    const uint64_t span = 1ull << 31;
+    for (uint64_t a = 3; a <= limit; a += span) {
+      uint64_t b = std::min<uint64_t>((uint64_t)limit + 1, a + span);
+      if ((rc = sieve_batch(e, a, b, e->seed_q.p, ns, ns_tiny, ns, nullptr, nullptr,
+                            e->base_q.p + filled)))
+        return rc;
+      CU(cudaMemcpyAsync(e->h_pinned, e->totals.p, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, e->st));
+      CU(cudaStreamSynchronize(e->st));
+      filled += e->h_pinned[0];
+    }
+    e->base_limit = limit;
+    e->base_count = (uint32_t)filled;
+  }
+  // counts for `limit` within the (possibly larger) table
+  uint32_t n = e->base_count;
+  if (e->base_limit > limit) {
+    // binary search on device values through small copies
+    uint32_t lo = 0, hi = e->base_count;  // find first index with q > limit
+    while (lo < hi) {
+      uint32_t mid = lo + (hi - lo) / 2;
+      uint32_t v;
+      CU(cudaMemcpy(&v, e->base_q.p + mid, 4, cudaMemcpyDeviceToHost));
+      if (v <= limit) lo = mid + 1; else hi = mid;
+    }
+    n = lo;
+  }
+  bt->nq = n;
+  bt->nq_tiny = std::min(n, count_le(e->host_seed, TINY_Q_LIMIT - 1));
+  bt->nq_seg = std::min(n, count_le(e->host_seed, SEG_BITS - 1));
+  return 0;
+}
+
+static int prepare_sieving_primes(pps_engine* e, uint32_t qmax, uint64_t pmax, const uint32_t** dq,
+                                  BaseTable* bt) {
+  // only q with q*q < pmax can matter
+  uint32_t lim = qmax;
+  const uint32_t r = isqrt64(pmax - 1);
+  if (r < lim) lim = r;
+  int which = ensure_base(e, lim, bt);
+  if (which < 0) return which;
+  *dq = which == 1 ? e->seed_q.p : e->base_q.p;
+  return PPS_OK;
+}
+
+extern "C" int pps_sieve_range(pps_engine* e, uint64_t lo, uint64_t hi, uint32_t qmax, uint64_t* out,
+                               size_t cap, size_t* count, uint64_t* sum) {
+  if (!e || hi <= lo || lo < 3) return set_err(PPS_ERR_INVALID_PARAM, "bad range");
+  CU(cudaSetDevice(e->device));
+  if (qmax == 0) {
+    qmax = 1u << 31;
+    if ((uint64_t)qmax * qmax > hi) qmax = (uint32_t)sqrt((double)hi);
+  }
+  const uint32_t* dq;
+  BaseTable bt;
+  int rc = prepare_sieving_primes(e, qmax, hi, &dq, &bt);
+  if (rc) return rc;
+  size_t total = 0;
+  uint64_t s = 0;
+  for (uint64_t a = lo | 1ull; a < hi; a += e->batch_span) {
+    uint64_t b = std::min(hi, a + e->batch_span);
+    const uint64_t nbits = (b - a + 1) / 2;
+    if ((rc = e->P.ensure(nbits / 2 + 64))) return rc;  // density of odd primes < 1/2 above 2^5
+    if ((rc = sieve_batch(e, a, b, dq, bt.nq, bt.nq_tiny, bt.nq_seg, e->P.p, nullptr, nullptr))) return rc;
+    CU(cudaMemcpyAsync(e->h_pinned, e->totals.p, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, e->st));
+    CU(cudaStreamSynchronize(e->st));
+    const uint64_t n = e->h_pinned[0];
+    s += e->h_pinned[1];
+    if (out && total < cap) {
+      size_t m = std::min<size_t>(n, cap - total);
+      CU(cudaMemcpy(out + total, e->P.p, m * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    }
+    total += n;
+  }
+  if (count) *count = total;
+  if (sum) *sum = s;
+  if (out && total > cap) return set_err(PPS_ERR_OVERFLOW, "%zu primes, buffer holds %zu", total, cap);
+  return PPS_OK;
+}
+
+// ------------------------------------------------------------------- walk
+static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
+  memset(a, 0, sizeof *a);
+  a->kmin = jp->kmin;
+  a->kmax = jp->kmax;
+  a->nmin = jp->nmin;
+  a->nmax = jp->nmax;
+  a->step = jp->step;
+  a->nsteps = (jp->nmax - jp->nmin + jp->step - 1) / jp->step;
+  if (jp->nmax == jp->nmin) a->nsteps = 0;
+  a->proth = jp->sign == 1 ? 1u : 0u;
+  // window pre-test parameters
+  const int kb = lg2u64(jp->kmax) + 1;         // kmax < 2^kb
+  const int lp = lg2u64(jp->pmin);
+  int u = (lp + kb - 64) / 2;
+  const int umin = kb > 32 ? kb - 32 : 0, umax = kb < 32 ? kb : 32;
+  if (u < umin) u = umin;
+  if (u > umax) u = umax;
+  const int t = 32 + u - kb;
+  a->win_hi = u >= 32 ? 0xffffffffu : ((1u << u) - 1u);
+  a->win_mask = t >= 32 ? 0xffffffffu : ((1u << t) - 1u);
+  a->kmax32 = jp->kmax < (1ull << 32) ? (uint32_t)jp->kmax : 0xffffffffu;
+}
+
+static int variant_ok(const pps_job_params* jp, int v) {
+  if (v == 1 && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
+  return 1;
+}
+
+static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64_t* dP, const uint64_t* dPinv,
+                    const uint64_t* d_np, uint64_t np_max, uint32_t idx_base, uint32_t nsteps_cap) {
+  WalkArgs a;
+  fill_walk_args(jp, &a);
+  if (nsteps_cap && a.nsteps > nsteps_cap) a.nsteps = nsteps_cap;
+  a.P = dP;
+  a.Pinv = dPinv;
+  a.d_np = d_np;
+  a.np = np_max;
+  a.idx_base = idx_base;
+  a.hits = e->hits.p;
+  a.hit_count = e->counters.p;
+  a.hit_cap = (uint32_t)std::min<size_t>(e->hits.n, 0xffffffffu);
+  const int threads = 256;
+  int maxb = walk_max_blocks(v, threads, jp->step, e->num_sms);
+  if (maxb <= 0) return set_err(PPS_ERR_CUDA, "walk variant %d unavailable", v);
+  uint64_t need = (np_max + threads - 1) / threads;
+  int blocks = (int)std::min<uint64_t>((uint64_t)maxb, need ? need : 1);
+  CU(launch_walk(v, a, blocks, threads, e->st));
+  e->launches++;
+  return PPS_OK;
+}
+
+// Time each walk variant on the first `np` resident primes with a capped n
+// range and keep the fastest for this step class.
+static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
+                    uint64_t np) {
+  const int cls = jp->step == 32 ? 1 : 0;
+  if (e->forced_variant >= 0) return e->forced_variant;
+  if (e->tuned_variant[cls] >= 0 && variant_ok(jp, e->tuned_variant[cls])) return e->tuned_variant[cls];
+  const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
+  const uint32_t cap_steps = 1024;
+  int best = 0;
+  float best_ms = 1e30f;
+  for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
+    if (!variant_ok(jp, v)) continue;
+    CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
+    int rc = run_walk(e, jp, v, dP, dPinv, nullptr, sample, 0, cap_steps);  // warm-up
+    if (rc) return rc;
+    CU(cudaEventRecord(e->ev[6], e->st));
+    for (int r = 0; r < 3; ++r)
+      if ((rc = run_walk(e, jp, v, dP, dPinv, nullptr, sample, 0, cap_steps))) return rc;
+    CU(cudaEventRecord(e->ev[7], e->st));
+    CU(cudaEventSynchronize(e->ev[7]));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
+  e->tuned_variant[cls] = best;
+  return best;
+}
+
+static int ensure_hit_buffers(pps_engine* e, size_t hit_cap, size_t fac_cap) {
+  int rc;
+  if ((rc = e->hits.ensure(hit_cap))) return rc;
+  if ((rc = e->factors.ensure(fac_cap))) return rc;
+  return PPS_OK;
+}
+
+static bool factor_less(const pps_factor& x, const pps_factor& y) {
+  if (x.p != y.p) return x.p < y.p;
+  if (x.k != y.k) return x.k < y.k;
+  if (x.n != y.n) return x.n < y.n;
+  return x.c < y.c;
+}
+
+// Filter the raw hits accumulated in e->hits and copy the factors out.
+static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap, size_t* nout,
+                      pps_job_stats* st, uint32_t* raw_hits_out, bool* overflow) {
+  CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
+  CU(cudaStreamSynchronize(e->st));
+  const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
+  *raw_hits_out = raw;
+  if (raw > e->hits.n) {
+    *overflow = true;
+    return PPS_OK;
+  }
+  FilterArgs f;
+  f.hits = e->hits.p;
+  f.d_nhits = e->counters.p;
+  f.hit_cap = (uint32_t)std::min<size_t>(e->hits.n, 0xffffffffu);
+  f.kstep = jp->kstep;
+  f.koffset = jp->koffset;
+  f.nmin = jp->nmin;
+  f.nmax = jp->nmax;
+  f.sign = jp->sign;
+  f.small_q = e->small_q.p;
+  f.nsmall = e->nsmall;
+  f.out = e->factors.p;
+  f.out_count = e->counters.p + 1;
+  f.out_cap = (uint32_t)std::min<size_t>(e->factors.n, 0xffffffffu);
+  CU(cudaEventRecord(e->ev[4], e->st));
+  if (raw) {
+    CU(launch_filter(f, raw, e->st));
+    e->launches++;
+  }
+  CU(cudaEventRecord(e->ev[5], e->st));
+  CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
+  CU(cudaStreamSynchronize(e->st));
+  const uint32_t nf = ((uint32_t*)e->h_pinned)[1];
+  float fms = 0;
+  CU(cudaEventElapsedTime(&fms, e->ev[4], e->ev[5]));
+  if (st) st->filter_ms += fms;
+  if (nf > e->factors.n) {
+    *overflow = true;
+    return PPS_OK;
+  }
+  std::vector<pps_factor> tmp(nf);
+  if (nf) CU(cudaMemcpy(tmp.data(), e->factors.p, nf * sizeof(pps_factor), cudaMemcpyDeviceToHost));
+  std::sort(tmp.begin(), tmp.end(), factor_less);
+  if (nout) *nout = nf;
+  if (out) memcpy(out, tmp.data(), std::min<size_t>(nf, cap) * sizeof(pps_factor));
+  if (st) st->factors = nf;
+  if (out && nf > cap) return set_err(PPS_ERR_OVERFLOW, "%u factors, buffer holds %zu", nf, cap);
+  if (!out && nf > 0 && cap > 0) return set_err(PPS_ERR_OVERFLOW, "null output buffer");
+  return PPS_OK;
+}
+
+static int run_job_once(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap, size_t* nout,
+                        pps_job_stats* st, bool* overflow) {
+  const uint32_t* dq;
+  BaseTable bt;
+  int rc = prepare_sieving_primes(e, jp->qmax, jp->pmax, &dq, &bt);
+  if (rc) return rc;
+  CU(cudaMemsetAsync(e->counters.p, 0, 2 * sizeof(uint32_t), e->st));
+  int variant = -1;
+  const uint64_t span = e->batch_span;
+  for (uint64_t a = jp->pmin | 1ull; a < jp->pmax; a += span) {
+    const uint64_t b = std::min(jp->pmax, a + span);
+    const uint64_t nbits = (b - a + 1) / 2;
+    // odd primes among nbits odd candidates above 2^32: density < 2/ln(2^32) < 0.1
+    const size_t pcap = (size_t)(nbits / 10) + 1024;
+    if ((rc = e->P.ensure(pcap))) return rc;
+    if ((rc = e->Pinv.ensure(pcap))) return rc;
+    CU(cudaEventRecord(e->ev[0], e->st));
+    if ((rc = sieve_batch(e, a, b, dq, bt.nq, bt.nq_tiny, bt.nq_seg, e->P.p, e->Pinv.p, nullptr))) return rc;
+    CU(cudaEventRecord(e->ev[1], e->st));
+    CU(cudaMemcpyAsync(e->h_pinned, e->totals.p, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, e->st));
+    CU(cudaStreamSynchronize(e->st));
+    const uint64_t np = e->h_pinned[0];
+    if (st) {
+      st->primes += np;
+      st->prime_sum += e->h_pinned[1];
+      st->batches++;
+    }
+    if (np == 0) continue;
+    if (variant < 0) {
+      variant = autotune(e, jp, e->P.p, e->Pinv.p, np);
+      if (variant < 0) return variant;
+      if (st) st->variant = (uint32_t)variant;
+    }
+    CU(cudaEventRecord(e->ev[2], e->st));
+    if ((rc = run_walk(e, jp, variant, e->P.p, e->Pinv.p, nullptr, np, 0, 0))) return rc;
+    CU(cudaEventRecord(e->ev[3], e->st));
+    if (st) {
+      CU(cudaEventSynchronize(e->ev[3]));
+      float ms0 = 0, ms1 = 0;
+      CU(cudaEventElapsedTime(&ms0, e->ev[0], e->ev[1]));
+      CU(cudaEventElapsedTime(&ms1, e->ev[2], e->ev[3]));
+      st->sieve_ms += ms0;
+      st->walk_ms += ms1;
+      const uint64_t nsteps = jp->nmax > jp->nmin ? (jp->nmax - jp->nmin + jp->step - 1) / jp->step : 0;
+      st->steps += np * nsteps;
+    }
+  }
+  uint32_t raw = 0;
+  rc = finish_job(e, jp, out, cap, nout, st, &raw, overflow);
+  if (st) st->raw_hits = raw;
+  return rc;
+}
+
+extern "C" int pps_run_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap,
+                           size_t* nout, pps_job_stats* st) {
+  if (!e || !jp) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  if (jp->step < 1 || jp->step > 32 || jp->pmin <= (1ull << 32)) return set_err(PPS_ERR_INVALID_PARAM, "job not normalized");
+  CU(cudaSetDevice(e->device));
+  size_t hit_cap = 1u << 20, fac_cap = 1u << 18;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    int rc = ensure_hit_buffers(e, std::max(hit_cap, e->hits.n), std::max(fac_cap, e->factors.n));
+    if (rc) return rc;
+    if (st) memset(st, 0, sizeof *st);
+    bool overflow = false;
+    cudaEventRecord(e->ev[6], e->st);
+    rc = run_job_once(e, jp, out, cap, nout, st, &overflow);
+    if (rc) return rc;
+    if (!overflow) {
+      cudaEventRecord(e->ev[7], e->st);
+      cudaEventSynchronize(e->ev[7]);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]);
+      if (st) st->total_ms = ms;
+      return PPS_OK;
+    }
+    hit_cap = e->hits.n * 4;
+    fac_cap = e->factors.n * 4;
+  }
+  return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "hit buffer overflow persisted");
+}
+
+// Walk primes already on the device; hits accumulate in e->hits.
+static int walk_device_list(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, size_t np,
+                            pps_job_stats* st) {
+  int variant = autotune(e, jp, dP, nullptr, np);
+  if (variant < 0) return variant;
+  if (st) st->variant = (uint32_t)variant;
+  CU(cudaEventRecord(e->ev[2], e->st));
+  int rc = run_walk(e, jp, variant, dP, nullptr, nullptr, np, 0, 0);
+  if (rc) return rc;
+  CU(cudaEventRecord(e->ev[3], e->st));
+  if (st) {
+    CU(cudaEventSynchronize(e->ev[3]));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]));
+    st->walk_ms += ms;
+    st->primes += np;
+    const uint64_t nsteps = jp->nmax > jp->nmin ? (jp->nmax - jp->nmin + jp->step - 1) / jp->step : 0;
+    st->steps += np * nsteps;
+  }
+  return PPS_OK;
+}
+
+extern "C" int pps_check_primes_device(pps_engine* e, const pps_job_params* jp, const uint64_t* d_P,
+                                       size_t np, pps_factor* out, size_t cap, size_t* nout,
+                                       pps_job_stats* st) {
+  if (!e || !jp || (!d_P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  CU(cudaSetDevice(e->device));
+  size_t hit_cap = 1u << 20, fac_cap = 1u << 18;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    int rc = ensure_hit_buffers(e, std::max(hit_cap, e->hits.n), std::max(fac_cap, e->factors.n));
+    if (rc) return rc;
+    if (st) memset(st, 0, sizeof *st);
+    CU(cudaMemsetAsync(e->counters.p, 0, 2 * sizeof(uint32_t), e->st));
+    if (np && (rc = walk_device_list(e, jp, d_P, np, st))) return rc;
+    bool overflow = false;
+    uint32_t raw = 0;
+    rc = finish_job(e, jp, out, cap, nout, st, &raw, &overflow);
+    if (st) st->raw_hits = raw;
+    if (rc || !overflow) return rc;
+    hit_cap = e->hits.n * 4;
+    fac_cap = e->factors.n * 4;
+  }
+  return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "hit buffer overflow persisted");
+}
+
+extern "C" int pps_check_primes(pps_engine* e, const pps_job_params* jp, const uint64_t* P, size_t np,
+                                pps_factor* out, size_t cap, size_t* nout, pps_job_stats* st) {
+  if (!e || !jp || (!P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  CU(cudaSetDevice(e->device));
+  int rc;
+  if ((rc = e->P.ensure(np ? np : 1))) return rc;
+  if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
+  return pps_check_primes_device(e, jp, e->P.p, np, out, cap, nout, st);
+}
+
+static bool hit_less(const pps_hit& x, const pps_hit& y) {
+  if (x.idx != y.idx) return x.idx < y.idx;
+  if (x.n != y.n) return x.n < y.n;
+  return x.k < y.k;
+}
+
+extern "C" int pps_check_primes_raw(pps_engine* e, const pps_job_params* jp, const uint64_t* P, size_t np,
+                                    pps_hit* out, size_t cap, size_t* nout) {
+  if (!e || !jp || (!P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  if (np > 0xffffffffull) return set_err(PPS_ERR_INVALID_PARAM, "too many primes for one call");
+  CU(cudaSetDevice(e->device));
+  int rc;
+  if ((rc = e->P.ensure(np ? np : 1))) return rc;
+  if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
+  size_t hit_cap = std::max<size_t>(1u << 20, e->hits.n);
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    if ((rc = ensure_hit_buffers(e, hit_cap, std::max<size_t>(1u << 18, e->factors.n)))) return rc;
+    CU(cudaMemsetAsync(e->counters.p, 0, 2 * sizeof(uint32_t), e->st));
+    if (np && (rc = walk_device_list(e, jp, e->P.p, np, nullptr))) return rc;
+    CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
+    CU(cudaStreamSynchronize(e->st));
+    const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
+    if (raw > e->hits.n) {
+      hit_cap = (size_t)raw * 2;
+      continue;
+    }
+    std::vector<pps_hit> tmp(raw);
+    if (raw) CU(cudaMemcpy(tmp.data(), e->hits.p, raw * sizeof(pps_hit), cudaMemcpyDeviceToHost));
+    std::sort(tmp.begin(), tmp.end(), hit_less);
+    if (nout) *nout = raw;
+    if (out) memcpy(out, tmp.data(), std::min<size_t>(raw, cap) * sizeof(pps_hit));
+    if (raw > cap) return set_err(PPS_ERR_OVERFLOW, "%u raw hits, buffer holds %zu", raw, cap);
+    return PPS_OK;
+  }
+  return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "hit buffer overflow persisted");
+}
+
+// ------------------------------------------------------------ IMAD probe
+extern "C" int pps_measure_imad_peak(pps_engine* e, double* mults_per_sec) {
+  if (!e || !mults_per_sec) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  CU(cudaSetDevice(e->device));
+  const int threads = 256, blocks = e->num_sms * 8;
+  int rc;
+  if ((rc = e->probe_sink.ensure((size_t)threads * blocks))) return rc;
+  const uint32_t iters = 1u << 16;
+  CU(launch_imad_probe(e->probe_sink.p, 1024, blocks, threads, e->st));  // warm-up
+  e->launches++;
+  CU(cudaEventRecord(e->ev[6], e->st));
+  CU(launch_imad_probe(e->probe_sink.p, iters, blocks, threads, e->st));
+  e->launches++;
+  CU(cudaEventRecord(e->ev[7], e->st));
+  CU(cudaEventSynchronize(e->ev[7]));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
+  const double mults = 3.0 * 4.0 * (double)iters * threads * blocks;
+  *mults_per_sec = mults / (ms * 1e-3);
+  return PPS_OK;
+}

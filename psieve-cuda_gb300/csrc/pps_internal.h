@@ -1,0 +1,88 @@
+// pps_internal.h -- kernel launchers and device-side structures shared by the
+// library's translation units.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ppsgpu.h"
+
+namespace pps {
+
+// ------------------------------------------------------------------ sieve
+// Odd candidates are numbered j = 0, 1, ... for values lo + 2j (lo odd).  One
+// CTA sieves one segment of SEG_BITS candidates in shared memory; primes
+// q >= SEG_BITS are scattered into the batch bitmap in global memory first.
+constexpr int SEG_LOG2 = 18;
+constexpr uint32_t SEG_BITS = 1u << SEG_LOG2;
+constexpr uint32_t SEG_WORDS = SEG_BITS / 32;
+constexpr int SIEVE_THREADS = 512;
+constexpr uint32_t TINY_Q_LIMIT = 128;  // q below this: whole CTA strides one q
+
+struct SieveBatch {
+  uint64_t lo;        // first odd candidate
+  uint64_t nbits;     // odd candidates in the batch
+  uint32_t nseg;      // ceil(nbits / SEG_BITS)
+  const uint32_t* q;  // sieving primes, ascending, odd, q <= qmax
+  uint32_t nq;        // number of sieving primes used (q*q < hi is checked too)
+  uint32_t nq_tiny;   // q < TINY_Q_LIMIT
+  uint32_t nq_seg;    // q < SEG_BITS (sieved per segment)
+  uint32_t* bitmap;   // nseg * SEG_WORDS words
+  uint32_t* seg_count;
+  uint32_t* seg_off;  // exclusive scan of seg_count
+  uint64_t* d_total;  // [0] = primes in batch (written by scan), [1] = wrapping sum
+};
+
+// Launch the full sieve of one batch on `st`: large-prime scatter, segment
+// sieve, scan, expansion into out64 (+ Montgomery constants into pinv64 when
+// non-null) or out32.  Returns the number of kernel launches issued.
+int launch_sieve_batch(const SieveBatch& b, uint64_t* out64, uint64_t* pinv64, uint32_t* out32,
+                       cudaStream_t st);
+
+// ------------------------------------------------------------------- walk
+struct WalkArgs {
+  const uint64_t* P;        // primes
+  const uint64_t* Pinv;     // -p^-1 mod 2^64 per prime, or null (computed)
+  const uint64_t* d_np;     // device-side prime count (or null: use np)
+  uint64_t np;
+  uint64_t kmin, kmax;
+  uint32_t nmin, nmax;
+  uint32_t step;            // s, 1..32
+  uint32_t nsteps;          // ceil((nmax - nmin) / s)
+  uint32_t proth;           // 1: K0 = p - 2^-nmin, 0: K0 = 2^-nmin
+  uint32_t win_hi;          // window pre-test: hi word <= win_hi ...
+  uint32_t win_mask;        // ... or (lo word & win_mask) == 0
+  uint32_t kmax32;          // low-bit pre-test (kmax < 2^32)
+  uint32_t idx_base;        // added to the prime index in hit records
+  pps_hit* hits;
+  uint32_t* hit_count;      // may exceed hit_cap: overflow is detected by host
+  uint32_t hit_cap;
+};
+
+// Variant v in [0, PPS_NUM_VARIANTS): step formulation x pre-test x unroll.
+const char* walk_variant_name(int v);
+// Largest useful grid for the walk kernel of variant v with `threads` threads
+// per block (occupancy-derived); 0 if the variant cannot run this step size.
+int walk_max_blocks(int v, int threads, uint32_t step, int num_sms);
+cudaError_t launch_walk(int v, const WalkArgs& a, int blocks, int threads, cudaStream_t st);
+
+// ----------------------------------------------------------------- filter
+struct FilterArgs {
+  const pps_hit* hits;
+  const uint32_t* d_nhits;  // device-side count (clamped to hit_cap inside)
+  uint32_t hit_cap;
+  uint64_t kstep, koffset;
+  uint32_t nmin, nmax;
+  int32_t sign;
+  const uint16_t* small_q;  // odd primes 3..32749
+  uint32_t nsmall;
+  pps_factor* out;
+  uint32_t* out_count;
+  uint32_t out_cap;
+};
+cudaError_t launch_filter(const FilterArgs& a, uint32_t max_hits, cudaStream_t st);
+
+// ------------------------------------------------------------- utilities
+cudaError_t launch_imad_probe(uint32_t* sink, uint32_t iters, int blocks, int threads,
+                              cudaStream_t st);
+
+}  // namespace pps

@@ -1,0 +1,432 @@
+// pps_kernels.cu -- sm_103a kernels of the PPSieve hot path.
+//
+//   k_sieve_large / k_sieve_seg / k_scan_counts / k_expand
+//       segmented sieve of Eratosthenes (reference: sieve.c:168-608 on the host).
+//       Candidates live as bits in shared memory; the primes and their
+//       Montgomery constants are written to HBM in order.
+//   k_walk<...>
+//       per-prime walk over n (reference: pps/appcu.cu:1120-1190 + 803-1115 for
+//       the flags, pps/app.c:1037-1121 for the exact (k, n)).  One thread owns
+//       one prime; 2^-nmin mod p by Montgomery exponentiation, then one
+//       reduction per `step` values of n, a cheap pre-test per step, and an
+//       exact count-trailing-zeros test on the rare candidates.  Hits are
+//       appended through one atomic per warp (ballot + popc ranks).
+//   k_filter
+//       output rule of pps/app.c:159-186 + pps/factor_proth.c:247-253 on the raw
+//       hits: one warp per hit, lanes split the odd primes below 32768.
+//   k_imad_probe
+//       multiply-pipe throughput probe on the walk's multiply mix.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pps_device.cuh"
+#include "pps_internal.h"
+
+namespace pps {
+
+// ===================================================================== sieve
+
+__device__ __forceinline__ uint64_t first_odd_multiple(uint64_t q, uint64_t lo) {
+  // smallest odd multiple of odd q that is >= max(lo, q*q); lo odd
+  uint64_t st = q * q;
+  if (st < lo) {
+    const uint64_t r = lo % q;
+    st = r ? lo + (q - r) : lo;
+    if ((st & 1ull) == 0ull) st += q;
+  }
+  return st;
+}
+
+// Primes q >= SEG_BITS hit a segment at most once: one thread per prime walks
+// its multiples through the whole batch and clears them in the global bitmap.
+__global__ void k_sieve_large(SieveBatch b) {
+  const uint64_t hi = b.lo + 2ull * b.nbits;
+  for (uint32_t i = b.nq_seg + blockIdx.x * blockDim.x + threadIdx.x; i < b.nq;
+       i += gridDim.x * blockDim.x) {
+    const uint64_t q = b.q[i];
+    if (q * q >= hi) continue;
+    const uint64_t st = first_odd_multiple(q, b.lo);
+    for (uint64_t j = (st - b.lo) >> 1; j < b.nbits; j += q)
+      atomicAnd(&b.bitmap[j >> 5], ~(1u << (j & 31u)));
+  }
+}
+
+__global__ void __launch_bounds__(SIEVE_THREADS) k_sieve_seg(SieveBatch b, int have_large) {
+  __shared__ uint32_t sb[SEG_WORDS];
+  __shared__ uint32_t warp_cnt[SIEVE_THREADS / 32];
+  const uint32_t seg = blockIdx.x;
+  const uint64_t seg_first = (uint64_t)seg * SEG_BITS;
+  const uint64_t left = b.nbits - seg_first;
+  const uint32_t bits = left < SEG_BITS ? (uint32_t)left : SEG_BITS;
+  const uint64_t seg_lo = b.lo + 2ull * seg_first;
+  const uint64_t seg_hi = seg_lo + 2ull * bits;
+  uint32_t* gw = b.bitmap + (size_t)seg * SEG_WORDS;
+
+  for (uint32_t w = threadIdx.x; w < SEG_WORDS; w += blockDim.x) {
+    uint32_t v = have_large ? gw[w] : 0xffffffffu;
+    const uint32_t j0 = w * 32u;
+    if (j0 >= bits) v = 0u;
+    else if (bits - j0 < 32u) v &= (1u << (bits - j0)) - 1u;
+    sb[w] = v;
+  }
+  __syncthreads();
+
+  // tiny primes: the CTA strides one q at a time
+  for (uint32_t i = 0; i < b.nq_tiny; ++i) {
+    const uint64_t q = b.q[i];
+    if (q * q >= seg_hi) break;
+    const uint64_t st = first_odd_multiple(q, seg_lo);
+    for (uint64_t j = ((st - seg_lo) >> 1) + (uint64_t)threadIdx.x * q; j < bits;
+         j += (uint64_t)blockDim.x * q)
+      atomicAnd(&sb[j >> 5], ~(1u << (j & 31u)));
+  }
+  // small primes: one thread per q
+  const uint32_t qend = b.nq_seg < b.nq ? b.nq_seg : b.nq;
+  for (uint32_t i = b.nq_tiny + threadIdx.x; i < qend; i += blockDim.x) {
+    const uint64_t q = b.q[i];
+    if (q * q >= seg_hi) continue;
+    const uint64_t st = first_odd_multiple(q, seg_lo);
+    const uint32_t qq = (uint32_t)q;
+    for (uint64_t j = (st - seg_lo) >> 1; j < bits; j += qq)
+      atomicAnd(&sb[j >> 5], ~(1u << (j & 31u)));
+  }
+  __syncthreads();
+
+  uint32_t cnt = 0;
+  for (uint32_t w = threadIdx.x; w < SEG_WORDS; w += blockDim.x) {
+    const uint32_t v = sb[w];
+    gw[w] = v;
+    cnt += __popc(v);
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += warp_cnt[i];
+    b.seg_count[seg] = t;
+  }
+}
+
+// Exclusive scan of the per-segment counts (one CTA).
+__global__ void __launch_bounds__(1024) k_scan_counts(const uint32_t* cnt, uint32_t* off, uint32_t n,
+                                                      uint64_t* d_total) {
+  __shared__ uint64_t part[1024];
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t a = threadIdx.x * per;
+  const uint32_t e = a + per < n ? a + per : n;
+  uint64_t s = 0;
+  for (uint32_t i = a; i < e; ++i) s += cnt[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t d = 1; d < blockDim.x; d <<= 1) {
+    const uint64_t v = threadIdx.x >= d ? part[threadIdx.x - d] : 0ull;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint64_t run = part[threadIdx.x] - s;
+  for (uint32_t i = a; i < e; ++i) {
+    off[i] = (uint32_t)run;
+    run += cnt[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) d_total[0] = part[threadIdx.x];
+}
+
+// One CTA per segment: rank the set bits and write the primes in order.
+template <bool OUT32>
+__global__ void __launch_bounds__(SIEVE_THREADS) k_expand(SieveBatch b, uint64_t* out64, uint64_t* pinv64,
+                                                          uint32_t* out32) {
+  constexpr uint32_t WPT = SEG_WORDS / SIEVE_THREADS;  // words per thread
+  __shared__ uint32_t warp_tot[SIEVE_THREADS / 32];
+  __shared__ unsigned long long blk_sum;
+  const uint32_t seg = blockIdx.x;
+  const uint32_t* gw = b.bitmap + (size_t)seg * SEG_WORDS + threadIdx.x * WPT;
+  const uint64_t base_val = b.lo + 2ull * ((uint64_t)seg * SEG_BITS + threadIdx.x * WPT * 32u);
+  uint32_t w[WPT];
+  uint32_t c = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < WPT; ++i) {
+    w[i] = gw[i];
+    c += __popc(w[i]);
+  }
+  // block exclusive scan of c
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  uint32_t inc = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc += v;
+  }
+  if (lane == 31) warp_tot[wid] = inc;
+  if (threadIdx.x == 0) blk_sum = 0ull;
+  __syncthreads();
+  uint32_t woff = 0;
+  for (uint32_t i = 0; i < wid; ++i) woff += warp_tot[i];
+  uint64_t pos = (uint64_t)b.seg_off[seg] + woff + inc - c;
+  uint64_t sum = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < WPT; ++i) {
+    uint32_t v = w[i];
+    while (v) {
+      const uint32_t bit = __ffs(v) - 1u;
+      v &= v - 1u;
+      const uint64_t p = base_val + 2ull * (i * 32u + bit);
+      sum += p;
+      if (OUT32) {
+        out32[pos] = (uint32_t)p;
+      } else {
+        out64[pos] = p;
+        if (pinv64) pinv64[pos] = neg_inv64(p);
+      }
+      ++pos;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  if (lane == 0) atomicAdd(&blk_sum, (unsigned long long)sum);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd((unsigned long long*)&b.d_total[1], blk_sum);
+}
+
+int launch_sieve_batch(const SieveBatch& b, uint64_t* out64, uint64_t* pinv64, uint32_t* out32,
+                       cudaStream_t st) {
+  int launches = 0;
+  const int have_large = b.nq > b.nq_seg;
+  if (have_large) {
+    cudaMemsetAsync(b.bitmap, 0xff, (size_t)b.nseg * SEG_WORDS * sizeof(uint32_t), st);
+    const uint32_t nl = b.nq - b.nq_seg;
+    uint32_t blocks = (nl + 255) / 256;
+    if (blocks > 65535u * 4u) blocks = 65535u * 4u;
+    k_sieve_large<<<blocks, 256, 0, st>>>(b);
+    ++launches;
+  }
+  k_sieve_seg<<<b.nseg, SIEVE_THREADS, 0, st>>>(b, have_large);
+  k_scan_counts<<<1, 1024, 0, st>>>(b.seg_count, b.seg_off, b.nseg, b.d_total);
+  if (out32)
+    k_expand<true><<<b.nseg, SIEVE_THREADS, 0, st>>>(b, nullptr, nullptr, out32);
+  else
+    k_expand<false><<<b.nseg, SIEVE_THREADS, 0, st>>>(b, out64, pinv64, nullptr);
+  launches += 3;
+  return launches;
+}
+
+// ====================================================================== walk
+
+// Pre-tests: never reject a true candidate K = k 2^i (k <= kmax, i < step).
+// Window: if i < t then K < kmax 2^t <= 2^(32+u), i.e. hi word < 2^u; otherwise
+// the low t bits are zero.  win_hi = 2^u - 1, win_mask = 2^t - 1, t = 32+u-bits(kmax).
+// Low bit: with 2^i the lowest set bit of the low word, K <= kmax 2^i implies
+// hi word <= hi32(kmax 2^i); a zero low word always passes.
+template <int TEST>
+__device__ __forceinline__ bool pretest(uint32_t klo, uint32_t khi, const WalkArgs& a) {
+  if (TEST == 0) {
+    return (khi <= a.win_hi) | ((klo & a.win_mask) == 0u);
+  } else {
+    const uint32_t lb = klo & (0u - klo);
+    return (lb == 0u) | (khi <= __umulhi(a.kmax32, lb));
+  }
+}
+
+__device__ __forceinline__ void exact_check(const WalkArgs& a, uint32_t klo, uint32_t khi, uint32_t n,
+                                            uint64_t p, uint32_t idx) {
+  const uint32_t i = klo ? (uint32_t)(__ffs(klo) - 1) : (uint32_t)(31 + __ffs(khi));
+  const uint64_t k = mk64(klo, khi) >> (i & 63u);
+  const bool hit = (i < a.step) && (k <= a.kmax) && (k >= a.kmin) && (n + i < a.nmax);
+  const unsigned act = __activemask();
+  const unsigned hm = __ballot_sync(act, hit);
+  if (hm) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(hm) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(a.hit_count, (uint32_t)__popc(hm));
+    base = __shfl_sync(act, base, leader);
+    if (hit) {
+      const uint32_t pos = base + (uint32_t)__popc(hm & ((1u << lane) - 1u));
+      if (pos < a.hit_cap) {
+        pps_hit h;
+        h.p = p;
+        h.k = k;
+        h.n = n + i;
+        h.idx = idx;
+        a.hits[pos] = h;
+      }
+    }
+  }
+}
+
+template <int FORM, bool S32>
+__device__ __forceinline__ void walk_step(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi,
+                                          uint32_t pinv_s, uint32_t s) {
+  if (FORM == 1 && S32) {
+    step_chain32(klo, khi, plo, phi, pinv_s);
+  } else if (FORM == 2) {
+    step_form2<S32>(klo, khi, plo, phi, pinv_s, s);
+  } else {
+    step_form0<S32>(klo, khi, plo, phi, pinv_s, s);
+  }
+}
+
+template <int FORM, int TEST, int UNROLL, bool S32>
+__global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
+  const uint64_t np = a.d_np ? *a.d_np : a.np;
+  const uint32_t s = S32 ? 32u : a.step;
+  for (uint64_t pi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pi < np;
+       pi += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t p = a.P[pi];
+    const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
+    const uint64_t x = inv_pow2(a.nmin, p, ps);
+    const uint64_t K = a.proth ? p - x : x;
+    uint32_t klo = lo32(K), khi = hi32(K);
+    const uint32_t plo = lo32(p), phi = hi32(p);
+    const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
+    const uint32_t idx = a.idx_base + (uint32_t)pi;
+    uint32_t n = a.nmin;
+    uint32_t t = 0;
+    for (; t + UNROLL <= a.nsteps; t += UNROLL) {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        if (pretest<TEST>(klo, khi, a)) exact_check(a, klo, khi, n + (uint32_t)u * s, p, idx);
+        walk_step<FORM, S32>(klo, khi, plo, phi, pinv_s, s);
+      }
+      n += (uint32_t)UNROLL * s;
+    }
+    for (; t < a.nsteps; ++t) {
+      if (pretest<TEST>(klo, khi, a)) exact_check(a, klo, khi, n, p, idx);
+      walk_step<FORM, S32>(klo, khi, plo, phi, pinv_s, s);
+      n += s;
+    }
+  }
+}
+
+struct VariantDesc {
+  const char* name;
+  int form, test, unroll;
+};
+static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
+    {"form0-window-u4", 0, 0, 4}, {"form0-lowbit-u4", 0, 1, 4}, {"chain-window-u4", 1, 0, 4},
+    {"form2-window-u4", 2, 0, 4}, {"form0-window-u8", 0, 0, 8}, {"form2-window-u8", 2, 0, 8},
+};
+
+const char* walk_variant_name(int v) {
+  return (v >= 0 && v < PPS_NUM_VARIANTS) ? kVariants[v].name : "?";
+}
+
+typedef void (*walk_fn)(WalkArgs);
+
+template <bool S32>
+static walk_fn pick(int v) {
+  switch (v) {
+    case 0: return k_walk<0, 0, 4, S32>;
+    case 1: return k_walk<0, 1, 4, S32>;
+    case 2: return k_walk<1, 0, 4, S32>;
+    case 3: return k_walk<2, 0, 4, S32>;
+    case 4: return k_walk<0, 0, 8, S32>;
+    case 5: return k_walk<2, 0, 8, S32>;
+  }
+  return nullptr;
+}
+
+int walk_max_blocks(int v, int threads, uint32_t step, int num_sms) {
+  walk_fn f = step == 32 ? pick<true>(v) : pick<false>(v);
+  if (!f) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, threads, 0) != cudaSuccess) return 0;
+  return per_sm * num_sms;
+}
+
+cudaError_t launch_walk(int v, const WalkArgs& a, int blocks, int threads, cudaStream_t st) {
+  walk_fn f = a.step == 32 ? pick<true>(v) : pick<false>(v);
+  if (!f || blocks <= 0) return cudaErrorInvalidValue;
+  f<<<blocks, threads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+// ==================================================================== filter
+
+__device__ __forceinline__ uint32_t pow2_mod_small(uint32_t e, uint32_t q) {
+  uint32_t r = 1u, b = 2u % q;
+  while (e) {
+    if (e & 1u) r = (r * b) % q;
+    b = (b * b) % q;
+    e >>= 1;
+  }
+  return r;
+}
+
+__global__ void k_filter(FilterArgs a) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  uint32_t nh = *a.d_nhits;
+  if (nh > a.hit_cap) nh = a.hit_cap;
+  for (uint32_t h = warp; h < nh; h += nwarps) {
+    const pps_hit x = a.hits[h];
+    bool ok = (x.k == a.kstep * (x.k / a.kstep) + a.koffset) && x.n >= a.nmin && x.n < a.nmax;
+    if (ok) {
+      bool div = false;
+      for (uint32_t base = 0; base < a.nsmall; base += 32u) {
+        const uint32_t i = base + lane;
+        if (i < a.nsmall) {
+          const uint32_t q = a.small_q[i];
+          const uint32_t kr = (uint32_t)(x.k % q);
+          const uint32_t t = (kr * pow2_mod_small(x.n, q)) % q;
+          div = ((t + (uint32_t)((int32_t)q + a.sign)) % q) == 0u;
+        }
+        if (__any_sync(0xffffffffu, div)) break;
+      }
+      ok = !__any_sync(0xffffffffu, div);
+    }
+    if (ok && lane == 0) {
+      const uint32_t pos = atomicAdd(a.out_count, 1u);
+      if (pos < a.out_cap) {
+        pps_factor f;
+        f.p = x.p;
+        f.k = x.k;
+        f.n = x.n;
+        f.c = a.sign;
+        a.out[pos] = f;
+      }
+    }
+  }
+}
+
+cudaError_t launch_filter(const FilterArgs& a, uint32_t max_hits, cudaStream_t st) {
+  uint32_t warps = max_hits ? max_hits : 1u;
+  uint32_t blocks = (warps * 32u + 255u) / 256u;
+  if (blocks > 4096u) blocks = 4096u;
+  k_filter<<<blocks, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+// ============================================================ multiply probe
+// Four independent chains per thread, each iteration one lo multiply, one
+// high multiply and one wide multiply-add (the walk step's mix) plus one xor.
+__global__ void __launch_bounds__(256) k_imad_probe(uint32_t* sink, uint32_t iters) {
+  uint32_t x0 = threadIdx.x * 2654435761u + 1u, x1 = x0 ^ 0x85ebca6bu, x2 = x0 ^ 0xc2b2ae35u,
+           x3 = x0 ^ 0x27d4eb2fu;
+  const uint32_t c1 = 0x9e3779b1u + blockIdx.x, c2 = 0x7f4a7c15u ^ blockIdx.x, c3 = 0x165667b1u;
+  uint64_t w0 = x0, w1 = x1, w2 = x2, w3 = x3;
+  for (uint32_t i = 0; i < iters; ++i) {
+#define PPS_PROBE_CHAIN(X, W)                      \
+  {                                                \
+    const uint32_t m = X * c1;                     \
+    const uint32_t h = __umulhi(m, c2);            \
+    W = (uint64_t)m * c3 + W;                      \
+    X = h ^ (uint32_t)(W >> 32);                   \
+  }
+    PPS_PROBE_CHAIN(x0, w0)
+    PPS_PROBE_CHAIN(x1, w1)
+    PPS_PROBE_CHAIN(x2, w2)
+    PPS_PROBE_CHAIN(x3, w3)
+#undef PPS_PROBE_CHAIN
+  }
+  const uint32_t r = x0 ^ x1 ^ x2 ^ x3 ^ (uint32_t)(w0 ^ w1 ^ w2 ^ w3);
+  if (r == 0x12345678u) sink[blockIdx.x * blockDim.x + threadIdx.x] = r;
+}
+
+cudaError_t launch_imad_probe(uint32_t* sink, uint32_t iters, int blocks, int threads,
+                              cudaStream_t st) {
+  k_imad_probe<<<blocks, threads, 0, st>>>(sink, iters);
+  return cudaGetLastError();
+}
+
+}  // namespace pps

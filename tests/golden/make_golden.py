@@ -1,0 +1,223 @@
+"""Generate the golden fixtures in tests/golden/ by running the REFERENCE itself.
+
+    make -C oracle ref                      # builds oracle/_ref/ from the reference sources
+    python tests/golden/make_golden.py      # (re)writes tests/golden/ref_cases.json, kat49.json
+
+Needs the reference checkout (REF, default /root/reference) only through the
+binaries that `make -C oracle ref` compiled into oracle/_ref/:
+  ppsieve_ref        the reference's main.c/sieve.c/pps/app.c/pps/factor_proth.c with
+                     the CPU stand-in for pps/appcu.h (every subsection flagged);
+  ppsieve_ref_fixed  the same with the 64-bit fix at pps/app.c:1087 (used where
+                     nstep >= 48, where the unfixed re-walk misses factors).
+Each case records the command line, the sorted factor lines and the reference's
+own prime fingerprint (count=, sum= from main.c:1232).  The fixtures are small
+text; the GPU machine never needs the reference.
+
+kat49.json holds planted factors for nstep >= 48 (p in [9999*2^48, 2^62)): p is a
+prime factor of k*2^n-1 or k*2^n+1 for small n found by factoring with sympy;
+each is then confirmed by running both reference binaries on a one-prime range.
+"""
+from __future__ import annotations
+
+import json
+import os
+import random
+import re
+import subprocess
+import sys
+import tempfile
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF_DIR = ROOT / "oracle" / "_ref"
+REF_BIN = REF_DIR / "ppsieve_ref"
+REF_FIXED = REF_DIR / "ppsieve_ref_fixed"
+
+FP_RE = re.compile(r"count=(\d+),sum=0x([0-9a-f]+)")
+
+
+def run_ref(args: list[str], fixed: bool = False, threads: int = 2) -> dict:
+    binary = REF_FIXED if fixed else REF_BIN
+    with tempfile.TemporaryDirectory() as td:
+        cmd = [str(binary), *args, f"-t{threads}", "-m8192", "-c1000000", "-r1000000", "-q",
+               "-fout.txt"]
+        t0 = time.time()
+        r = subprocess.run(cmd, cwd=td, capture_output=True, text=True)
+        dt = time.time() - t0
+        out = Path(td, "out.txt")
+        lines = [l.strip() for l in out.read_text().splitlines() if "|" in l] if out.exists() else []
+    m = FP_RE.search(r.stderr)
+    res = {"args": args, "binary": binary.name, "rc": r.returncode, "seconds": round(dt, 2),
+           "lines": sorted(lines), "unique": len(set(lines)), "total": len(lines)}
+    if m:
+        res["count"] = int(m.group(1))
+        res["sum"] = "0x" + m.group(2)
+    if r.returncode != 0:
+        res["stderr_tail"] = r.stderr[-400:]
+    return res
+
+
+def fixed_cases() -> list[tuple[str, list[str], bool]]:
+    c = []
+    c.append(("c1_full", ["-p1e12", "-P1000200000000", "-k1201", "-K9999", "-n2000", "-N3000"], False))
+    c.append(("many_n_test", ["-p42070e9", "-P42070050e6", "-k1201", "-K9999", "-N2000000"], False))
+    base = 42 * 10**12
+    for i, off in enumerate([0, 25 * 10**9, 50 * 10**9, 75 * 10**9, 10**11 - 2 * 10**6]):
+        lo = base + off
+        c.append((f"c2_slice{i}", [f"-p{lo}", f"-P{lo + 2 * 10**6}", "-k1201", "-K9999",
+                                    "-n2000000", "-N3000000"], False))
+    lo3 = (1 << 62) - (1 << 34)
+    c.append(("c3_slice_lo", [f"-p{lo3}", f"-P{lo3 + 10**7}", "-k3", "-K9999", "-n100000",
+                              "-N1000000", "-R"], True))
+    c.append(("c3_slice_hi", [f"-p{(1 << 62) - 10**7}", f"-P{1 << 62}", "-k3", "-K9999",
+                              "-n100000", "-N1000000", "-R"], True))
+    # Riesel, small p, many factors
+    c.append(("riesel_small", ["-p1e12", "-P1000050000000", "-k1201", "-K9999", "-n2000",
+                               "-N3000", "-R"], False))
+    # kstep / koffset generality (-M -s), pps/app.c:595-604
+    c.append(("kstep6_off3", ["-p1e12", "-P1000050000000", "-k3", "-K9999", "-n2000", "-N4000",
+                              "-M6", "-s3"], False))
+    # pseudo-prime mode: sieve only with q < 1000 (main.c:971-972 -Q)
+    c.append(("qmax_1000", ["-p1e12", "-P1000001000000", "-k1201", "-K9999", "-n2000",
+                            "-N3000", "-Q1000"], False))
+    # rejected by the reference: auto nmin = 62 < 64 (pps/app.c:683-694, pps/appcu.cu:195)
+    c.append(("kround_nauto", ["-p5e11", "-P500020000000", "-k1200", "-K10000", "-N3000"], False))
+    # rejected: nstep clamped to nmax-nmin+1 = 11 makes 2^(64-11) > pmin (pps/appcu.cu:160-176)
+    c.append(("nstep_clamp", ["-p1e12", "-P1000100000000", "-k1201", "-K9999", "-n2000",
+                              "-N2010"], False))
+    # even kmin/kmax round to kstep*b+koffset (pps/app.c:705-708)
+    c.append(("kround", ["-p1e12", "-P1000050000000", "-k1200", "-K10000", "-n2000", "-N3000"],
+              False))
+    # nmin from 2*lg2(pmin)-lg2(kmax)-1 (pps/app.c:683-694): 72 here
+    c.append(("nmin_auto", ["-p1e13", "-P10000020000000", "-k1201", "-K9999", "-N5000"], False))
+    # nstep clamped to nmax-nmin+1 = 10 and still valid at this pmin
+    c.append(("nstep_clamp_ok", ["-p2000000000000000000", "-P2000000000010000000", "-k3", "-K9999",
+                                 "-n1000", "-N1009"], False))
+    # kmin == kmax
+    c.append(("single_k", ["-p1e12", "-P1000500000000", "-k9475", "-K9475", "-n2000",
+                           "-N9000"], False))
+    return c
+
+
+def random_jobs(seed: int = 20240501, count: int = 40) -> list[tuple[str, list[str], bool]]:
+    """Small seeded jobs with the mixed-job distribution's shape (sides, k and n
+    widths, p log-uniform), shrunk so the reference finishes each in seconds."""
+    rng = random.Random(seed)
+    jobs = []
+    while len(jobs) < count:
+        side = rng.choice([1, -1])
+        kmin = rng.randrange(3, 5001) | 1
+        kw = int(10 ** rng.uniform(2, 4))
+        kmax = kmin + kw
+        nmin = rng.randrange(1000, 200000)
+        nw = int(10 ** rng.uniform(2, 4.3))
+        nmax = nmin + nw
+        if len(jobs) % 3 == 2:
+            pmin = int(10 ** rng.uniform(14, 18.3))
+            pw = int(10 ** rng.uniform(5, 6.3))
+        else:
+            pmin = int(10 ** rng.uniform(11.8, 14))
+            pw = int(10 ** rng.uniform(6, 6.7))
+            kw = int(10 ** rng.uniform(3, 4))
+            kmax = kmin + kw
+            nw = int(10 ** rng.uniform(3.5, 4.5))
+            nmax = nmin + nw
+        # valid only if the reference's rules accept it (pps/appcu.cu:163)
+        ks = (kmax // 2) * 2 + 1
+        nstep = 1
+        while (ks << nstep) < pmin:
+            nstep += 1
+        nstep = min(nstep, nmax - nmin + 1)
+        if (1 << (64 - nstep)) > pmin or pmin <= (1 << 32):
+            continue
+        args = [f"-p{pmin}", f"-P{pmin + pw}", f"-k{kmin}", f"-K{kmax}", f"-n{nmin}", f"-N{nmax}"]
+        if side < 0:
+            args.append("-R")
+        jobs.append((f"rand{len(jobs):02d}", args, nstep >= 48))
+    return jobs
+
+
+def planted_kat49(max_found: int = 8, seed: int = 7) -> list[dict]:
+    import sympy
+
+    lo, hi = 9999 << 48, 1 << 62
+    rng = random.Random(seed)
+    found = []
+    tried = 0
+    while len(found) < max_found and tried < 20000:
+        tried += 1
+        n = rng.randrange(64, 84)
+        k = rng.randrange(3, 10000) | 1
+        c = rng.choice([1, -1])
+        N = k * (1 << n) + c
+        f = sympy.factorint(N, limit=1 << 22)
+        for q, e in f.items():
+            if lo <= q < hi and sympy.isprime(q):
+                found.append({"p": int(q), "k": k, "n": n, "c": c})
+        if tried % 500 == 0:
+            print(f"  kat49: tried {tried}, found {len(found)}", flush=True)
+    return found
+
+
+def main() -> None:
+    if not REF_BIN.exists() or not REF_FIXED.exists():
+        sys.exit("build the reference first: make -C oracle ref")
+    which = sys.argv[1:] or ["cases", "kat"]
+    only = set(which[1:]) if which and which[0] == "cases" else set()
+    if "cases" in which:
+        cases = fixed_cases() + random_jobs()
+        if only:
+            cases = [c for c in cases if c[0] in only or (c[0].startswith("rand") and "rand" in only)]
+        out_json = HERE / "ref_cases.json"
+        results = json.loads(out_json.read_text()) if (only and out_json.exists()) else {}
+        if only:
+            for k in list(results):
+                if k.startswith("rand") and "rand" in only:
+                    del results[k]
+        heavy = {"many_n_test", "c1_full", "c3_slice_lo", "c3_slice_hi"}
+
+        def one(case):
+            name, args, fixed = case
+            t = 8 if name in heavy else 2
+            r = run_ref(args, fixed=fixed, threads=t)
+            print(f"{name}: {r['total']} lines in {r['seconds']} s rc={r['rc']}", flush=True)
+            return name, r
+
+        light = [c for c in cases if c[0] not in heavy]
+        with ThreadPoolExecutor(max_workers=3) as ex:
+            for name, r in ex.map(one, light):
+                results[name] = r
+        for c in cases:
+            if c[0] in heavy:
+                name, r = one(c)
+                results[name] = r
+        if not only:
+            # as-is reference on the nstep>=48 slice too, to record its divergence
+            lo3 = (1 << 62) - (1 << 34)
+            r = run_ref([f"-p{lo3}", f"-P{lo3 + 10**7}", "-k3", "-K9999", "-n100000", "-N1000000",
+                         "-R"], fixed=False, threads=8)
+            results["c3_slice_lo_asis"] = r
+        out_json.write_text(json.dumps(results, indent=1, sort_keys=True))
+    if "kat" in which:
+        kats = planted_kat49()
+        out = []
+        for kat in kats:
+            p = kat["p"]
+            # nmin/nmax around n with nstep = 49: kmax*2^48 < pmin
+            nmin, nmax = 64, 160
+            args = [f"-p{p}", f"-P{p + 2}", "-k3", "-K9999", f"-n{nmin}", f"-N{nmax}"]
+            if kat["c"] < 0:
+                args.append("-R")
+            rf = run_ref(args, fixed=True, threads=1)
+            ra = run_ref(args, fixed=False, threads=1)
+            out.append({**kat, "args": args, "fixed_lines": rf["lines"], "asis_lines": ra["lines"]})
+            print(f"kat p={p} k={kat['k']} n={kat['n']} c={kat['c']}: fixed {len(rf['lines'])} "
+                  f"as-is {len(ra['lines'])}", flush=True)
+        (HERE / "kat49.json").write_text(json.dumps(out, indent=1, sort_keys=True))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's own
+outputs (tests/golden/ref_cases.json, produced by running the reference) and
+against the CPU oracle on seeded inputs.  Integer work: bit-exact."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import args_to_spec, lines_of
+
+pytestmark = pytest.mark.gpu
+
+FAST_CASES = ["c1_full", "many_n_test", "c2_slice0", "c2_slice1", "c2_slice2", "c2_slice3",
+              "c2_slice4", "c3_slice_lo", "c3_slice_hi", "riesel_small", "kstep6_off3", "qmax_1000",
+              "kround_nauto", "nstep_clamp", "single_k"]
+
+
+def _gpu_lines(pps, engine, spec):
+    jp = pps.normalize(**spec)
+    fac, st = engine.run_job(jp)
+    return lines_of(pps.factors_to_tuples(fac)), st
+
+
+@pytest.mark.parametrize("name", FAST_CASES)
+def test_reference_cases(pps, engine, ref_cases, name):
+    case = ref_cases[name]
+    spec = args_to_spec(case["args"])
+    got, st = _gpu_lines(pps, engine, spec)
+    assert got == sorted(set(case["lines"])), name
+    if "count" in case:
+        assert st.primes == case["count"]
+        assert st.prime_sum == int(case["sum"], 16)
+
+
+def test_reference_random_jobs(pps, engine, ref_cases):
+    names = sorted(k for k in ref_cases if k.startswith("rand"))
+    assert names
+    for name in names:
+        case = ref_cases[name]
+        got, st = _gpu_lines(pps, engine, args_to_spec(case["args"]))
+        assert got == sorted(set(case["lines"])), name
+        assert st.primes == case["count"], name
+
+
+def test_kat49_planted(pps, engine, kat49):
+    for kat in kat49:
+        spec = args_to_spec(kat["args"])
+        got, _ = _gpu_lines(pps, engine, spec)
+        assert got == sorted(set(kat["fixed_lines"])), kat
+        want = f"{kat['p']} | {kat['k']}*2^{kat['n']}{kat['c']:+d}"
+        # the planted factor is reported unless the output rule drops it
+        if want in kat["fixed_lines"]:
+            assert want in got
+
+
+@pytest.mark.parametrize("variant", list(range(6)))
+def test_every_walk_variant_matches_oracle(pps, engine, ora, variant):
+    specs = [
+        dict(pmin=10**12, pmax=10**12 + 3 * 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=5000),
+        dict(pmin=42 * 10**12, pmax=42 * 10**12 + 3 * 10**6, kmin=1201, kmax=9999, nmin=2000000,
+             nmax=2040000),
+        dict(pmin=(1 << 62) - (1 << 26), pmax=(1 << 62) - (1 << 26) + 2 * 10**6, kmin=3, kmax=9999,
+             nmin=100000, nmax=140000, sign=-1),
+    ]
+    engine.set_variant(variant)
+    try:
+        for spec in specs:
+            got, st = _gpu_lines(pps, engine, spec)
+            want, cnt, _ = ora.run(ora.normalize(**spec))
+            assert got == lines_of(ora.tuples(want)), (variant, spec)
+            assert st.primes == cnt
+    finally:
+        engine.set_variant(-1)
+
+
+def test_sieve_matches_oracle(engine, ora):
+    rng = np.random.default_rng(5)
+    for _ in range(6):
+        lo = int(rng.integers(2**33, 2**61))
+        hi = lo + int(rng.integers(1, 3 * 10**6))
+        qmax = int(np.sqrt(hi)) + 1
+        got, n, s = engine.sieve_range(lo, hi, qmax, want_primes=True)
+        want = ora.sieve_range(lo, hi, qmax)
+        assert n == len(want)
+        assert np.array_equal(got, want)
+        assert s == int(want.astype(np.uint64).sum(dtype=np.uint64))
+
+
+def test_sieve_pseudoprime_mode(engine, ora):
+    lo, hi, qmax = 10**12, 10**12 + 10**6, 1000
+    got, n, _ = engine.sieve_range(lo, hi, qmax, want_primes=True)
+    want = ora.sieve_range(lo, hi, qmax)
+    assert np.array_equal(got, want)
+
+
+def test_sieve_base_primes_large_qmax(engine, ora):
+    # sieving primes beyond the host seed table are made on the device
+    lo = (1 << 62) - 4 * 10**6
+    got, n, _ = engine.sieve_range(lo, 1 << 62, 0, want_primes=True)
+    want = ora.sieve_range(lo, 1 << 62, int(np.sqrt(float(1 << 62))))
+    assert np.array_equal(got, want)
+
+
+def test_check_host_primes_matches_oracle(pps, engine, ora):
+    spec = dict(pmin=10**12, pmax=10**12 + 10**8, kmin=1201, kmax=9999, nmin=2000, nmax=3000)
+    jp = pps.normalize(**spec)
+    primes = ora.sieve_range(spec["pmin"], spec["pmax"], jp.qmax)
+    fac, st = engine.check_primes(jp, primes)
+    want = ora.walk_list(ora.normalize(**spec), primes)
+    assert pps.factors_to_tuples(fac) == ora.tuples(want)
+    assert st.primes == len(primes)
+
+
+def test_raw_hits_cover_factors(pps, engine, ora):
+    spec = dict(pmin=10**12, pmax=10**12 + 5 * 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=3000)
+    jp = pps.normalize(**spec)
+    primes = ora.sieve_range(spec["pmin"], spec["pmax"], jp.qmax)
+    raw = engine.check_primes_raw(jp, primes)
+    fac, _ = engine.check_primes(jp, primes)
+    rawset = {(int(h["p"]), int(h["k"]), int(h["n"])) for h in raw}
+    for f in fac:
+        assert (int(f["p"]), int(f["k"]), int(f["n"])) in rawset
+    for h in raw:
+        p, k, n = int(h["p"]), int(h["k"]), int(h["n"])
+        assert primes[int(h["idx"])] == p
+        assert ora.kpow_mod(k, n, 1, p) == 0
+        assert jp.kmin <= k <= jp.kmax and jp.nmin <= n < jp.nmax
+
+
+def test_empty_and_degenerate(pps, engine, ora):
+    # no primes at all in range
+    jp = pps.normalize(pmin=10**12 + 40, pmax=10**12 + 60, kmin=1201, kmax=9999, nmin=2000, nmax=3000)
+    fac, st = engine.run_job(jp)
+    assert len(fac) == 0
+    # nmin == nmax: the reference clamps nstep to 1 and then requires 2^63 <= pmin,
+    # so an empty n range is always rejected (pps/appcu.cu:160-176)
+    with pytest.raises(pps.PPSError) as ei:
+        pps.normalize(pmin=10**12, pmax=10**12 + 10**6, kmin=1201, kmax=9999, nmin=2000, nmax=2000)
+    assert ei.value.code == pps.PPS_ERR_INVALID_PARAM
+    # the shortest valid n range at the top of the p range: nstep clamped to 3
+    lo = (1 << 62) - 10**6
+    spec = dict(pmin=lo, pmax=1 << 62, kmin=3, kmax=9999, nmin=1000, nmax=1002, sign=-1)
+    jp = pps.normalize(**spec)
+    assert jp.nstep == 3
+    fac, st = engine.run_job(jp)
+    want, cnt, _ = ora.run(ora.normalize(**spec))
+    assert pps.factors_to_tuples(fac) == ora.tuples(want) and st.primes == cnt
+    # empty prime list through the host-list entry point
+    fac, st = engine.check_primes(jp, np.zeros(0, dtype=np.uint64))
+    assert len(fac) == 0
+
+
+def test_batch_span_does_not_change_results(pps, engine, ora):
+    spec = dict(pmin=10**12, pmax=10**12 + 2 * 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=6000)
+    jp = pps.normalize(**spec)
+    base, _ = engine.run_job(jp)
+    engine.set_batch_span(1 << 21)
+    try:
+        small, st = engine.run_job(jp)
+    finally:
+        engine.set_batch_span(1 << 31)
+    assert st.batches > 5
+    assert np.array_equal(base, small)
+
+
+def test_c2_large_slice_per_line(pps, engine, ora):
+    """Size-independent property at a large size: every reported line is a true
+    factor with the output rule satisfied, and the prime fingerprint matches the
+    oracle's sieve."""
+    lo = 42 * 10**12 + 10**10
+    spec = dict(pmin=lo, pmax=lo + 2 * 10**8, kmin=1201, kmax=9999, nmin=2000000, nmax=3000000)
+    jp = pps.normalize(**spec)
+    fac, st = engine.run_job(jp)
+    for p, k, n, c in pps.factors_to_tuples(fac):
+        assert ora.verify_line(p, k, n, c)
+        assert ora.small_factor(k, n, c) == 0
+        assert 1201 <= k <= 9999 and 2000000 <= n < 3000000
+    primes = ora.sieve_range(lo, lo + 2 * 10**8, jp.qmax)
+    assert st.primes == len(primes)
+    assert st.prime_sum == int(primes.sum(dtype=np.uint64))
