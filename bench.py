@@ -253,7 +253,8 @@ def run_gpu(args) -> None:
         host_sets = []
         for i in range(need):
             jp = slice_params(seq[i])
-            pr, n, _ = eng.sieve_range(jp.pmin, jp.pmax, jp.qmax, want_primes=True)
+            est = int(1.2 * (jp.pmax - jp.pmin) / np.log(float(jp.pmin))) + 4096
+            pr, n, _ = eng.sieve_range(jp.pmin, jp.pmax, jp.qmax, want_primes=True, cap=est)
             pin = torch.empty(n, dtype=torch.int64, pin_memory=True)
             pin.numpy().view(np.uint64)[:] = pr
             host_sets.append((jp, pin))
@@ -320,6 +321,44 @@ def run_gpu(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+def run_profile(args) -> None:
+    """One job on a reduced slice with a forced walk variant (for ncu captures):
+    exactly one k_walk launch per job."""
+    import ppsgpu
+
+    eng = ppsgpu.Engine(0)
+    eng.set_variant(args.variant)
+    spec = dict(C2, pmax=C2["pmin"] + args.profile[0], nmax=C2["nmin"] + args.profile[1])
+    for _ in range(args.profile_reps):
+        fac, st = eng.run_job(ppsgpu.normalize(**spec))
+        print(f"profile job: {st.primes} primes, {st.steps} steps, walk {st.walk_ms:.3f} ms, "
+              f"{len(fac)} factors", flush=True)
+    eng.close()
+
+
+def run_sweep(args) -> None:
+    """Walk rate of every kernel variant on the first slice (stderr report)."""
+    import ppsgpu
+
+    eng = ppsgpu.Engine(0)
+    spec = dict(C2, pmax=C2["pmin"] + args.sweep_span, nmax=C2["nmin"] + args.sweep_nwidth)
+    jp = ppsgpu.normalize(**spec)
+    res = {}
+    for v in range(ppsgpu.PPS_NUM_VARIANTS):
+        eng.set_variant(v)
+        eng.run_job(jp)
+        best = None
+        for _ in range(3):
+            _, st = eng.run_job(jp)
+            rate = st.steps / (st.walk_ms * 1e-3)
+            best = max(best or 0, rate)
+        res[v] = best
+        print(f"variant {v}: {best:.4e} walk steps/s ({3 * best / 1e12:.3f} Tmul/s)", flush=True)
+    print(f"imad peak: {eng.imad_peak() / 1e12:.3f} Tmul/s", flush=True)
+    print(json.dumps({"sweep": res}), flush=True)
+    eng.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -329,8 +368,18 @@ def main() -> None:
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", type=int, nargs=2, metavar=("SPAN", "NWIDTH"))
+    ap.add_argument("--profile-reps", type=int, default=1)
+    ap.add_argument("--variant", type=int, default=5)
+    ap.add_argument("--sweep", action="store_true")
+    ap.add_argument("--sweep-span", type=int, default=1 << 28)
+    ap.add_argument("--sweep-nwidth", type=int, default=100000)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.sweep:
+        run_sweep(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

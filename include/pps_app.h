@@ -1,0 +1,55 @@
+/* pps_app.h -- the application plugin hooks served by the GPU plugin
+   (psieve-cuda_gb300/host/app_gpu.c, object _build/app_gpu.o).
+
+   Same names, arguments, return values and error behaviour as the reference's
+   plugin interface pps/app.h:73-96 (Ken-g6/PSieve-CUDA), so the reference's
+   main.c and sieve.c link against this plugin in place of pps/app.c +
+   pps/appcu.cu + pps/factor_proth.c.  The plugin reads main.c's globals
+   (main.h:57-60) and reports fatal errors through main.c's bexit().
+
+   Behaviour differences (by design; outputs are the same lines):
+     - the device returns exact (p, k, n) and applies the output rule of
+       pps/app.c:159-186 itself, so there is no CPU re-walk of flagged primes;
+     - app_thread_fun1() does not pad a partial batch with composites;
+     - -i (input sieve file) is rejected with ERR_NOT_IMPLEMENTED.
+*/
+#ifndef PPS_APP_H
+#define PPS_APP_H
+
+#include <stdint.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPS_APP_SHORT_OPTS "k:K:n:N:i:f:b:d:m:M:s:R"
+
+/* pps/app.h:73-84 */
+void app_banner(void);
+int app_parse_option(int opt, char *arg, const char *source);
+void app_help(void);
+void app_init(void);
+unsigned int app_thread_init(int th);
+void app_thread_fun(int th, const uint64_t *P, uint64_t *lastP, const unsigned int cthread_count);
+void app_thread_fun1(int th, uint64_t *P, uint64_t *lastP, const unsigned int cthread_count,
+                     unsigned int len);
+void app_thread_fini(int th);
+int app_read_checkpoint(FILE *f);
+void app_write_checkpoint(FILE *f);
+void app_fini(uint64_t pstop);
+
+/* pps/app.h:85-96 */
+struct n_subsection {
+  unsigned int n_subsection_start[9];
+  unsigned int *first_n_subsection;
+};
+extern struct n_subsection *thread_subsections;
+extern unsigned int nmin, nmax;
+extern int search_proth;
+extern uint64_t kmax, kmin;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

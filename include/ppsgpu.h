@@ -116,12 +116,15 @@ void pps_engine_destroy(pps_engine *e);
 /* Device memory held by the engine, in bytes. */
 uint64_t pps_engine_device_bytes(const pps_engine *e);
 
+/* Streaming multiprocessors of the engine's device. */
+int pps_engine_sm_count(const pps_engine *e);
+
 /* Batch width of the p-range per device sieve batch (default 2^31).  Smaller
    batches lower memory; results do not depend on it. */
 int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 
 /* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
-#define PPS_NUM_VARIANTS 6
+#define PPS_NUM_VARIANTS 10
 int pps_engine_set_variant(pps_engine *e, int variant);
 
 /* Whole job: device sieve of [pmin,pmax), walk, filter.  Factors are sorted by

@@ -59,6 +59,9 @@ def load() -> ctypes.CDLL:
         lib.ppo_walk_list.restype = ctypes.c_long
         lib.ppo_walk_list.argtypes = [P(Params), P(ctypes.c_uint64), ctypes.c_size_t, ctypes.c_int,
                                       ctypes.c_void_p, ctypes.c_size_t]
+        lib.ppo_walk_prime_raw.restype = ctypes.c_size_t
+        lib.ppo_walk_prime_raw.argtypes = [P(Params), ctypes.c_uint64, ctypes.c_void_p,
+                                           ctypes.c_size_t]
         lib.ppo_small_factor.restype = ctypes.c_uint32
         lib.ppo_small_factor.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32]
         lib.ppo_small_factor_from.restype = ctypes.c_uint32
@@ -122,6 +125,19 @@ def walk_list(params: Params, primes, nthreads: int | None = None, cap: int = 1 
             cap = n
             continue
         return out[:n].copy()
+
+
+def raw_candidates(params: Params, primes) -> list[tuple[int, int, int]]:
+    """(p, k, n) before the output filter, for every prime in the list."""
+    lib = load()
+    out = np.zeros(256, dtype=FACTOR_DTYPE)
+    res = []
+    for p in primes:
+        n = lib.ppo_walk_prime_raw(ctypes.byref(params), int(p),
+                                   out.ctypes.data_as(ctypes.c_void_p), len(out))
+        assert n <= len(out)
+        res.extend((int(r["p"]), int(r["k"]), int(r["n"])) for r in out[:n])
+    return res
 
 
 def sieve_range(lo: int, hi: int, qmax: int) -> np.ndarray:

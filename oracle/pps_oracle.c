@@ -226,6 +226,33 @@ size_t ppo_walk_prime(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t 
   return found;
 }
 
+/* Raw candidates of one prime before the output filter: k in [kmin, kmax],
+   nmin <= n < nmax (what sets a flag bit in pps/appcu.cu:803-1115).  Same walk
+   as ppo_walk_prime; c is set to the job's sign. */
+size_t ppo_walk_prime_raw(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t cap)
+{
+  size_t found = 0;
+  const uint64_t ps = neg_inv64(p);
+  uint64_t k = powmod64((p + 1) / 2, pp->nmin, p);
+  if (pp->c == 1) k = p - k;
+  uint32_t n = pp->nmin;
+  const uint32_t s = pp->nstep;
+  do {
+    int i = __builtin_ctzll(k);
+    uint64_t kk = k >> i;
+    if (kk <= pp->kmax && kk >= pp->kmin && (uint32_t)i < s && n + (uint32_t)i < pp->nmax) {
+      if (found < cap) {
+        out[found].p = p; out[found].k = kk;
+        out[found].n = n + (uint32_t)i; out[found].c = pp->c;
+      }
+      found++;
+    }
+    n += s;
+    k = shift_down(k, p, ps, s);
+  } while (n < pp->nmax);
+  return found;
+}
+
 /* ------------------------------------------------------------------ sieve */
 
 typedef struct {

@@ -59,6 +59,9 @@ int ppo_normalize(ppo_params *out, uint64_t pmin, uint64_t pmax, uint64_t kmin,
    number of factors found (may exceed cap). */
 size_t ppo_walk_prime(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t cap);
 
+/* Raw candidates of one prime before the output filter (k in range, n < nmax). */
+size_t ppo_walk_prime_raw(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t cap);
+
 /* The output filter alone (test_factor): 1 if the line would be printed. */
 int ppo_test_factor(const ppo_params *pp, uint64_t k, uint32_t n, int32_t c);
 

@@ -85,15 +85,17 @@ def build(verbose: bool = False) -> dict[str, Path]:
                   f"-L{OUT}", "-lppsgpu", "-Xlinker", "-rpath,$ORIGIN", "-lcudart"])
         out["libppsgpu_appcu"] = clib
 
-    # host plugin (app.h hooks) as a static archive + object for drivers to link
+    # host plugin (the app.h hooks, include/pps_app.h) as a shared library; it
+    # resolves main.c's globals (pmin, pmax, bexit, ...) from the executable
     plugin_src = HOST / "app_gpu.c"
     if plugin_src.exists():
-        pobj = OUT / "app_gpu.o"
-        deps = [plugin_src] + sorted(HOST.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
-        if _stale(pobj, deps):
-            _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-fPIC", f"-I{INCLUDE}", f"-I{HOST}",
-                  "-c", str(plugin_src), "-o", str(pobj)])
-        out["app_gpu_obj"] = pobj
+        plib = OUT / "libppsgpu_app.so"
+        deps = [plugin_src, lib] + sorted(HOST.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+        if _stale(plib, deps):
+            _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-Wextra", "-fPIC", "-shared",
+                  f"-I{INCLUDE}", f"-I{HOST}", str(plugin_src), "-o", str(plib), f"-L{OUT}",
+                  "-lppsgpu", "-Wl,-rpath,$ORIGIN", "-lpthread"])
+        out["libppsgpu_app"] = plib
     return out
 
 

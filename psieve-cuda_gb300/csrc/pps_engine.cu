@@ -258,6 +258,8 @@ extern "C" uint64_t pps_engine_device_bytes(const pps_engine* e) {
          e->factors.bytes() + e->counters.bytes() + e->small_q.bytes() + e->probe_sink.bytes();
 }
 
+extern "C" int pps_engine_sm_count(const pps_engine* e) { return e ? e->num_sms : 0; }
+
 extern "C" int pps_engine_set_batch_span(pps_engine* e, uint64_t span) {
   if (!e || span < 2ull * SEG_BITS) return set_err(PPS_ERR_INVALID_PARAM, "batch span too small");
   e->batch_span = span & ~1ull;
@@ -442,7 +444,7 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
 }
 
 static int variant_ok(const pps_job_params* jp, int v) {
-  if (v == 1 && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
+  if ((v == 7 || v == 8) && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
   return 1;
 }
 

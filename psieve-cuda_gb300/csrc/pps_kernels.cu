@@ -265,33 +265,91 @@ __device__ __forceinline__ void walk_step(uint32_t& klo, uint32_t& khi, uint32_t
   }
 }
 
-template <int FORM, int TEST, int UNROLL, bool S32>
+// One thread walks ILP primes side by side.  With BLOCK, the pre-test result is
+// OR-ed into a flag over U unrolled steps and only a flagged block is replayed
+// from its saved starting value with the exact test (the replay recomputes the
+// same values, so the walk continues from the already computed end value).
+// Without BLOCK the pre-test branches every step.
+template <int FORM, int TEST, int U, bool S32, int ILP, bool BLOCK>
 __global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
   const uint64_t np = a.d_np ? *a.d_np : a.np;
   const uint32_t s = S32 ? 32u : a.step;
-  for (uint64_t pi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pi < np;
-       pi += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t p = a.P[pi];
-    const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
-    const uint64_t x = inv_pow2(a.nmin, p, ps);
-    const uint64_t K = a.proth ? p - x : x;
-    uint32_t klo = lo32(K), khi = hi32(K);
-    const uint32_t plo = lo32(p), phi = hi32(p);
-    const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
-    const uint32_t idx = a.idx_base + (uint32_t)pi;
+  const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; base < np;
+       base += gstride * ILP) {
+    uint32_t klo[ILP], khi[ILP], plo[ILP], phi[ILP], pinv_s[ILP], idx[ILP];
+    uint64_t p[ILP];
+    bool valid[ILP];
+#pragma unroll
+    for (int j = 0; j < ILP; ++j) {
+      const uint64_t pi = base + (uint64_t)j * gstride;
+      valid[j] = pi < np;
+      p[j] = a.P[valid[j] ? pi : base];
+      const uint64_t ps = a.Pinv ? a.Pinv[valid[j] ? pi : base] : neg_inv64(p[j]);
+      const uint64_t x = inv_pow2(a.nmin, p[j], ps);
+      const uint64_t K = a.proth ? p[j] - x : x;
+      klo[j] = lo32(K);
+      khi[j] = hi32(K);
+      plo[j] = lo32(p[j]);
+      phi[j] = hi32(p[j]);
+      pinv_s[j] = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
+      idx[j] = a.idx_base + (uint32_t)pi;
+    }
     uint32_t n = a.nmin;
     uint32_t t = 0;
-    for (; t + UNROLL <= a.nsteps; t += UNROLL) {
+    for (; t + U <= a.nsteps; t += U) {
+      if (BLOCK) {
+        uint32_t slo[ILP], shi[ILP];
+        bool f[ILP];
 #pragma unroll
-      for (int u = 0; u < UNROLL; ++u) {
-        if (pretest<TEST>(klo, khi, a)) exact_check(a, klo, khi, n + (uint32_t)u * s, p, idx);
-        walk_step<FORM, S32>(klo, khi, plo, phi, pinv_s, s);
+        for (int j = 0; j < ILP; ++j) {
+          slo[j] = klo[j];
+          shi[j] = khi[j];
+          f[j] = false;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+          for (int j = 0; j < ILP; ++j) {
+            f[j] |= pretest<TEST>(klo[j], khi[j], a);
+            walk_step<FORM, S32>(klo[j], khi[j], plo[j], phi[j], pinv_s[j], s);
+          }
+        }
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < ILP; ++j) any |= f[j] & valid[j];
+        if (any) {
+#pragma unroll
+          for (int j = 0; j < ILP; ++j) {
+            if (f[j] && valid[j]) {
+              uint32_t rlo = slo[j], rhi = shi[j];
+#pragma unroll 1
+              for (int u = 0; u < U; ++u) {
+                if (pretest<TEST>(rlo, rhi, a)) exact_check(a, rlo, rhi, n + (uint32_t)u * s, p[j], idx[j]);
+                walk_step<FORM, S32>(rlo, rhi, plo[j], phi[j], pinv_s[j], s);
+              }
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+          for (int j = 0; j < ILP; ++j) {
+            if (valid[j] && pretest<TEST>(klo[j], khi[j], a))
+              exact_check(a, klo[j], khi[j], n + (uint32_t)u * s, p[j], idx[j]);
+            walk_step<FORM, S32>(klo[j], khi[j], plo[j], phi[j], pinv_s[j], s);
+          }
+        }
       }
-      n += (uint32_t)UNROLL * s;
+      n += (uint32_t)U * s;
     }
     for (; t < a.nsteps; ++t) {
-      if (pretest<TEST>(klo, khi, a)) exact_check(a, klo, khi, n, p, idx);
-      walk_step<FORM, S32>(klo, khi, plo, phi, pinv_s, s);
+#pragma unroll
+      for (int j = 0; j < ILP; ++j) {
+        if (valid[j] && pretest<TEST>(klo[j], khi[j], a)) exact_check(a, klo[j], khi[j], n, p[j], idx[j]);
+        walk_step<FORM, S32>(klo[j], khi[j], plo[j], phi[j], pinv_s[j], s);
+      }
       n += s;
     }
   }
@@ -299,11 +357,12 @@ __global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
 
 struct VariantDesc {
   const char* name;
-  int form, test, unroll;
 };
 static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
-    {"form0-window-u4", 0, 0, 4}, {"form0-lowbit-u4", 0, 1, 4}, {"chain-window-u4", 1, 0, 4},
-    {"form2-window-u4", 2, 0, 4}, {"form0-window-u8", 0, 0, 8}, {"form2-window-u8", 2, 0, 8},
+    {"form0-window-u4-step"}, {"chain-window-u4-step"}, {"chain-window-u8-block"},
+    {"form2-window-u8-block"}, {"form0-window-u8-block"}, {"chain-window-u8-block-ilp2"},
+    {"form2-window-u8-block-ilp2"}, {"chain-lowbit-u8-block"}, {"form0-lowbit-u8-block"},
+    {"chain-window-u16-block"},
 };
 
 const char* walk_variant_name(int v) {
@@ -315,12 +374,16 @@ typedef void (*walk_fn)(WalkArgs);
 template <bool S32>
 static walk_fn pick(int v) {
   switch (v) {
-    case 0: return k_walk<0, 0, 4, S32>;
-    case 1: return k_walk<0, 1, 4, S32>;
-    case 2: return k_walk<1, 0, 4, S32>;
-    case 3: return k_walk<2, 0, 4, S32>;
-    case 4: return k_walk<0, 0, 8, S32>;
-    case 5: return k_walk<2, 0, 8, S32>;
+    case 0: return k_walk<0, 0, 4, S32, 1, false>;
+    case 1: return k_walk<1, 0, 4, S32, 1, false>;
+    case 2: return k_walk<1, 0, 8, S32, 1, true>;
+    case 3: return k_walk<2, 0, 8, S32, 1, true>;
+    case 4: return k_walk<0, 0, 8, S32, 1, true>;
+    case 5: return k_walk<1, 0, 8, S32, 2, true>;
+    case 6: return k_walk<2, 0, 8, S32, 2, true>;
+    case 7: return k_walk<1, 1, 8, S32, 1, true>;
+    case 8: return k_walk<0, 1, 8, S32, 1, true>;
+    case 9: return k_walk<1, 0, 16, S32, 1, true>;
   }
   return nullptr;
 }

@@ -154,6 +154,8 @@ def planted_kat49(max_found: int = 8, seed: int = 7) -> list[dict]:
         c = rng.choice([1, -1])
         N = k * (1 << n) + c
         f = sympy.factorint(N, limit=1 << 22)
+        if min(f) < 32768:
+            continue  # the output rule would drop the line (pps/app.c:171-179)
         for q, e in f.items():
             if lo <= q < hi and sympy.isprime(q):
                 found.append({"p": int(q), "k": k, "n": n, "c": c})
@@ -201,6 +203,18 @@ def main() -> None:
                          "-R"], fixed=False, threads=8)
             results["c3_slice_lo_asis"] = r
         out_json.write_text(json.dumps(results, indent=1, sort_keys=True))
+    if "files" in which:
+        # The reference's own golden lists, sorted: pps/oldsort.txt (the older,
+        # unfiltered many_n_test.sh output) and pps/pps_test_ok.txt; and the
+        # many_n_test.sh range as the current reference prints it (from its run).
+        ref_root = Path(os.environ.get("PPS_REFERENCE", "/root/reference"))
+        for src, dst in (("pps/oldsort.txt", "oldsort_144.txt"),
+                         ("pps/pps_test_ok.txt", "pps_test_ok_15.txt")):
+            lines = sorted(l.strip() for l in (ref_root / src).read_text().splitlines()
+                           if "|" in l)
+            (HERE / dst).write_text("\n".join(lines) + "\n")
+        cases = json.loads((HERE / "ref_cases.json").read_text())
+        (HERE / "many_n_test_39.txt").write_text("\n".join(cases["many_n_test"]["lines"]) + "\n")
     if "kat" in which:
         kats = planted_kat49()
         out = []

@@ -1,0 +1,66 @@
+"""The app.h plugin (libppsgpu_app.so) on the GPU, driven in main.c's calling
+order (tests/harness/plugin_driver.c): the factor file it writes must equal the
+reference's own output for the same options."""
+from __future__ import annotations
+
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from helpers import args_to_spec
+
+ROOT = Path(__file__).resolve().parent.parent
+HARNESS = ROOT / "tests" / "harness" / "plugin_driver.c"
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def driver(pps, tmp_path_factory):
+    out = tmp_path_factory.mktemp("plugin") / "plugin_driver"
+    libdir = Path(pps.LIB_PATH).parent
+    subprocess.run(["gcc", "-O2", "-std=gnu11", f"-I{ROOT / 'include'}", str(HARNESS), "-o",
+                    str(out), f"-L{libdir}", "-lppsgpu_app", "-lppsgpu", f"-Wl,-rpath,{libdir}"],
+                   check=True)
+    return out
+
+
+@pytest.mark.parametrize("name", ["c1_full", "many_n_test", "riesel_small", "kstep6_off3",
+                                  "c2_slice2"])
+def test_plugin_factor_file(driver, tmp_path, ora, ref_cases, name):
+    case = ref_cases[name]
+    spec = args_to_spec(case["args"])
+    params = ora.normalize(**spec)
+    primes = ora.sieve_range(params.pmin, params.pmax, params.qmax)
+    pf = tmp_path / "primes.bin"
+    primes.astype("<u8").tofile(pf)
+    ff = tmp_path / "factors.txt"
+    args = [a for a in case["args"] if not a.startswith(("-p", "-P"))]
+    r = subprocess.run([str(driver), str(pf), f"-p{params.pmin}", f"-P{params.pmax}", *args,
+                        f"-f{ff}", "-m1"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr
+    assert "checkpoint_ok=1" in r.stdout
+    lines = sorted(l for l in ff.read_text().splitlines() if "|" in l) if ff.exists() else []
+    assert lines == case["lines"]
+    assert f"count={case['count']}," in r.stdout
+    n = len(lines)
+    assert f"Found {n} factor{'' if n == 1 else 's'}" in r.stdout
+
+
+def test_plugin_rejects_input_file(driver, tmp_path):
+    pf = tmp_path / "p.bin"
+    pf.write_bytes(b"")
+    r = subprocess.run([str(driver), str(pf), "-p1000000000000", "-P1000000100000", "-k1201",
+                        "-K9999", "-n2000", "-N3000", "-iabcd.txt"], capture_output=True, text=True)
+    assert r.returncode == 3 and "bexit(-150)" in r.stderr
+
+
+def test_plugin_rejects_like_reference(driver, tmp_path):
+    pf = tmp_path / "p.bin"
+    pf.write_bytes(b"")
+    # kmax >= pmin (pps/app.c:671-675)
+    r = subprocess.run([str(driver), str(pf), "-p1000000000000", "-P1000000100000", "-k1201",
+                        "-K1000000000001", "-n2000", "-N3000"], capture_output=True, text=True)
+    assert r.returncode == 3 and "bexit(-178)" in r.stderr
+    assert "kmax < pmin" in r.stderr
