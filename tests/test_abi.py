@@ -40,11 +40,11 @@ def test_libppsgpu_exports_header(built, pps):
 
 
 def test_every_header_is_exported(built, pps):
-    libs = [pps.LIB_PATH, pps.COMPAT_LIB_PATH]
+    libs = [pps.LIB_PATH, pps.COMPAT_LIB_PATH, Path(pps.LIB_PATH).parent / "libppsgpu_app.so"]
     syms = set()
     for lib in libs:
-        if lib.exists():
-            syms |= _exported(lib)
+        assert lib.exists(), lib
+        syms |= _exported(lib)
     for h in sorted(INCLUDE.glob("*.h")):
         missing = [s for s in _declared(h) if s not in syms]
         assert not missing, (h.name, missing)
