@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 FAST_CASES = ["c1_full", "many_n_test", "c2_slice0", "c2_slice1", "c2_slice2", "c2_slice3",
               "c2_slice4", "c3_slice_lo", "c3_slice_hi", "riesel_small", "kstep6_off3", "qmax_1000",
-              "kround_nauto", "nstep_clamp", "single_k"]
+              "kround", "nmin_auto", "nstep_clamp_ok", "single_k"]
 
 
 def _gpu_lines(pps, engine, spec):
