@@ -352,6 +352,9 @@ def run_sweep(args) -> None:
             _, st = eng.run_job(jp)
             rate = st.steps / (st.walk_ms * 1e-3)
             best = max(best or 0, rate)
+        if st.variant != v:
+            print(f"variant {v}: not exact for this job (ran {st.variant})", flush=True)
+            continue
         res[v] = best
         print(f"variant {v}: {best:.4e} walk steps/s ({3 * best / 1e12:.3f} Tmul/s)", flush=True)
     print(f"imad peak: {eng.imad_peak() / 1e12:.3f} Tmul/s", flush=True)

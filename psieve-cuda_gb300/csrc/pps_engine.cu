@@ -441,10 +441,21 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
   a->win_hi = u >= 32 ? 0xffffffffu : ((1u << u) - 1u);
   a->win_mask = t >= 32 ? 0xffffffffu : ((1u << t) - 1u);
   a->kmax32 = jp->kmax < (1ull << 32) ? (uint32_t)jp->kmax : 0xffffffffu;
+  a->bound_hi = jp->kmax < (1ull << 32) ? (uint32_t)(jp->kmax >> 1) : 0xffffffffu;
 }
 
 static int variant_ok(const pps_job_params* jp, int v) {
   if ((v == 7 || v == 8) && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
+  if (v >= 10 && jp->step != 32) return 0;                       // lean kernels: 32-bit steps
+  if (v == 10 || v == 13) {                                       // running-minimum window: u == 0
+    WalkArgs a;
+    fill_walk_args(jp, &a);
+    if (a.win_hi != 0) return 0;
+  }
+  if (v == 12 || v == 14) {  // single bound: kmax < 2^32 and a false-pass rate below 2^-12
+    if (jp->kmax >= (1ull << 32)) return 0;
+    if (jp->pmin / jp->kmax < (1ull << 43)) return 0;
+  }
   return 1;
 }
 
@@ -476,7 +487,10 @@ static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
                     uint64_t np) {
   const int cls = jp->step == 32 ? 1 : 0;
-  if (e->forced_variant >= 0) return e->forced_variant;
+  // a forced variant is honoured only where it is exact for this job
+  if (e->forced_variant >= 0 && variant_ok(jp, e->forced_variant) &&
+      walk_max_blocks(e->forced_variant, 256, jp->step, e->num_sms) > 0)
+    return e->forced_variant;
   if (e->tuned_variant[cls] >= 0 && variant_ok(jp, e->tuned_variant[cls])) return e->tuned_variant[cls];
   const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
   const uint32_t cap_steps = 1024;

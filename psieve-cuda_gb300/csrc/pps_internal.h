@@ -52,6 +52,7 @@ struct WalkArgs {
   uint32_t win_hi;          // window pre-test: hi word <= win_hi ...
   uint32_t win_mask;        // ... or (lo word & win_mask) == 0
   uint32_t kmax32;          // low-bit pre-test (kmax < 2^32)
+  uint32_t bound_hi;        // single-bound pre-test: hi word <= bound_hi
   uint32_t idx_base;        // added to the prime index in hit records
   pps_hit* hits;
   uint32_t* hit_count;      // may exceed hit_cap: overflow is detected by host

@@ -355,6 +355,57 @@ __global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
   }
 }
 
+// ---- lean 32-bit-step walk (step == 32, the large-n configurations).
+// The exact re-check of a flagged block lives in a separate non-inlined
+// function so that the hot loop keeps few live registers.
+__device__ __forceinline__ void replay_block32(const WalkArgs& a, uint32_t klo, uint32_t khi, uint32_t plo,
+                                            uint32_t phi, uint32_t pinv, uint32_t n, uint32_t nblk,
+                                            uint64_t p, uint32_t idx) {
+  for (uint32_t u = 0; u < nblk; ++u) {
+    exact_check(a, klo, khi, n + 32u * u, p, idx);
+    step_chain32(klo, khi, plo, phi, pinv);
+  }
+}
+
+// TEST 0: window via a running minimum (valid when win_hi == 0): a candidate has
+//         hi word 0 or low-word bits under win_mask all zero, so min(hi, lo & mask)
+//         is 0 at it; the block is flagged when the minimum over it is 0.
+// TEST 1: window, general form (hi <= win_hi or (lo & win_mask) == 0).
+// TEST 2: single bound (valid when p > kmax 2^43): a candidate K = k 2^i with i < 32
+//         has hi word <= floor(kmax 2^31 / 2^32) = win_hi.
+template <int TEST, int U>
+__global__ void __launch_bounds__(256) k_walk32(WalkArgs a) {
+  const uint64_t np = a.d_np ? *a.d_np : a.np;
+  const uint32_t win_hi = a.win_hi, win_mask = a.win_mask, bound_hi = a.bound_hi;
+  const uint32_t nsteps = a.nsteps, nmin = a.nmin;
+  const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t pi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pi < np; pi += gstride) {
+    const uint64_t p = a.P[pi];
+    const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
+    const uint64_t x = inv_pow2(nmin, p, ps);
+    const uint64_t K = a.proth ? p - x : x;
+    uint32_t klo = lo32(K), khi = hi32(K);
+    const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
+    uint32_t t = 0;
+    for (; t + U <= nsteps; t += U) {
+      const uint32_t slo = klo, shi = khi;
+      uint32_t acc = 0xffffffffu;
+      bool f = false;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (TEST == 0) acc = min(acc, min(khi, klo & win_mask));
+        else if (TEST == 1) f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
+        else f |= khi <= bound_hi;
+        step_chain32(klo, khi, plo, phi, pinv);
+      }
+      if (TEST == 0) f = acc == 0u;
+      if (f) replay_block32(a, slo, shi, plo, phi, pinv, nmin + 32u * t, U, p, a.idx_base + (uint32_t)pi);
+    }
+    if (t < nsteps)
+      replay_block32(a, klo, khi, plo, phi, pinv, nmin + 32u * t, nsteps - t, p, a.idx_base + (uint32_t)pi);
+  }
+}
+
 struct VariantDesc {
   const char* name;
 };
@@ -362,7 +413,8 @@ static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
     {"form0-window-u4-step"}, {"chain-window-u4-step"}, {"chain-window-u8-block"},
     {"form2-window-u8-block"}, {"form0-window-u8-block"}, {"chain-window-u8-block-ilp2"},
     {"form2-window-u8-block-ilp2"}, {"chain-lowbit-u8-block"}, {"form0-lowbit-u8-block"},
-    {"chain-window-u16-block"},
+    {"chain-window-u16-block"}, {"lean-min-u8"}, {"lean-window-u8"}, {"lean-bound-u8"},
+    {"lean-min-u16"}, {"lean-bound-u16"},
 };
 
 const char* walk_variant_name(int v) {
@@ -384,6 +436,11 @@ static walk_fn pick(int v) {
     case 7: return k_walk<1, 1, 8, S32, 1, true>;
     case 8: return k_walk<0, 1, 8, S32, 1, true>;
     case 9: return k_walk<1, 0, 16, S32, 1, true>;
+    case 10: return S32 ? k_walk32<0, 8> : nullptr;
+    case 11: return S32 ? k_walk32<1, 8> : nullptr;
+    case 12: return S32 ? k_walk32<2, 8> : nullptr;
+    case 13: return S32 ? k_walk32<0, 16> : nullptr;
+    case 14: return S32 ? k_walk32<2, 16> : nullptr;
   }
   return nullptr;
 }
