@@ -358,11 +358,34 @@ __global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
 // ---- lean 32-bit-step walk (step == 32, the large-n configurations).
 // The exact re-check of a flagged block lives in a separate non-inlined
 // function so that the hot loop keeps few live registers.
-__device__ __forceinline__ void replay_block32(const WalkArgs& a, uint32_t klo, uint32_t khi, uint32_t plo,
-                                            uint32_t phi, uint32_t pinv, uint32_t n, uint32_t nblk,
-                                            uint64_t p, uint32_t idx) {
-  for (uint32_t u = 0; u < nblk; ++u) {
-    exact_check(a, klo, khi, n + 32u * u, p, idx);
+__device__ __noinline__ void replay_block32(uint32_t klo, uint32_t khi, uint32_t plo, uint32_t phi,
+                                            uint32_t pinv, uint32_t n, uint32_t nblk, uint64_t p,
+                                            uint32_t idx, uint64_t kmin, uint64_t kmax, uint32_t nmax,
+                                            pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
+  for (uint32_t u = 0; u < nblk; ++u, n += 32u) {
+    const uint32_t i = klo ? (uint32_t)(__ffs(klo) - 1) : (uint32_t)(31 + __ffs(khi));
+    const uint64_t k = mk64(klo, khi) >> (i & 63u);
+    const bool hit = (i < 32u) && (k <= kmax) && (k >= kmin) && (n + i < nmax);
+    const unsigned act = __activemask();
+    const unsigned hm = __ballot_sync(act, hit);
+    if (hm) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(hm) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(hit_count, (uint32_t)__popc(hm));
+      base = __shfl_sync(act, base, leader);
+      if (hit) {
+        const uint32_t pos = base + (uint32_t)__popc(hm & ((1u << lane) - 1u));
+        if (pos < hit_cap) {
+          pps_hit h;
+          h.p = p;
+          h.k = k;
+          h.n = n + i;
+          h.idx = idx;
+          hits[pos] = h;
+        }
+      }
+    }
     step_chain32(klo, khi, plo, phi, pinv);
   }
 }
@@ -374,7 +397,7 @@ __device__ __forceinline__ void replay_block32(const WalkArgs& a, uint32_t klo, 
 // TEST 2: single bound (valid when p > kmax 2^43): a candidate K = k 2^i with i < 32
 //         has hi word <= floor(kmax 2^31 / 2^32) = win_hi.
 template <int TEST, int U>
-__global__ void __launch_bounds__(256) k_walk32(WalkArgs a) {
+__global__ void __launch_bounds__(256, 8) k_walk32(WalkArgs a) {
   const uint64_t np = a.d_np ? *a.d_np : a.np;
   const uint32_t win_hi = a.win_hi, win_mask = a.win_mask, bound_hi = a.bound_hi;
   const uint32_t nsteps = a.nsteps, nmin = a.nmin;
@@ -399,10 +422,14 @@ __global__ void __launch_bounds__(256) k_walk32(WalkArgs a) {
         step_chain32(klo, khi, plo, phi, pinv);
       }
       if (TEST == 0) f = acc == 0u;
-      if (f) replay_block32(a, slo, shi, plo, phi, pinv, nmin + 32u * t, U, p, a.idx_base + (uint32_t)pi);
+      if (f)
+        replay_block32(slo, shi, plo, phi, pinv, nmin + 32u * t, U, p, a.idx_base + (uint32_t)pi,
+                       a.kmin, a.kmax, a.nmax, a.hits, a.hit_count, a.hit_cap);
     }
     if (t < nsteps)
-      replay_block32(a, klo, khi, plo, phi, pinv, nmin + 32u * t, nsteps - t, p, a.idx_base + (uint32_t)pi);
+      replay_block32(klo, khi, plo, phi, pinv, nmin + 32u * t, nsteps - t, p,
+                     a.idx_base + (uint32_t)pi, a.kmin, a.kmax, a.nmax, a.hits, a.hit_count,
+                     a.hit_cap);
   }
 }
 
