@@ -447,12 +447,12 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
 static int variant_ok(const pps_job_params* jp, int v) {
   if ((v == 7 || v == 8) && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
   if (v >= 10 && jp->step != 32) return 0;                       // lean kernels: 32-bit steps
-  if (v == 10 || v == 13) {                                       // running-minimum window: u == 0
+  if (v == 10 || v == 13 || v == 15) {                            // running-minimum window: u == 0
     WalkArgs a;
     fill_walk_args(jp, &a);
     if (a.win_hi != 0) return 0;
   }
-  if (v == 12 || v == 14) {  // single bound: kmax < 2^32 and a false-pass rate below 2^-12
+  if (v == 12 || v == 14 || v == 16) {  // single bound: kmax < 2^32, false-pass rate below 2^-12
     if (jp->kmax >= (1ull << 32)) return 0;
     if (jp->pmin / jp->kmax < (1ull << 43)) return 0;
   }

@@ -355,81 +355,130 @@ __global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
   }
 }
 
-// ---- lean 32-bit-step walk (step == 32, the large-n configurations).
-// The exact re-check of a flagged block lives in a separate non-inlined
-// function so that the hot loop keeps few live registers.
-__device__ __noinline__ void replay_block32(uint32_t klo, uint32_t khi, uint32_t plo, uint32_t phi,
-                                            uint32_t pinv, uint32_t n, uint32_t nblk, uint64_t p,
-                                            uint32_t idx, uint64_t kmin, uint64_t kmax, uint32_t nmax,
-                                            pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
-  for (uint32_t u = 0; u < nblk; ++u, n += 32u) {
-    const uint32_t i = klo ? (uint32_t)(__ffs(klo) - 1) : (uint32_t)(31 + __ffs(khi));
-    const uint64_t k = mk64(klo, khi) >> (i & 63u);
-    const bool hit = (i < 32u) && (k <= kmax) && (k >= kmin) && (n + i < nmax);
-    const unsigned act = __activemask();
-    const unsigned hm = __ballot_sync(act, hit);
-    if (hm) {
-      const int lane = threadIdx.x & 31;
-      const int leader = __ffs(hm) - 1;
-      uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(hit_count, (uint32_t)__popc(hm));
-      base = __shfl_sync(act, base, leader);
-      if (hit) {
-        const uint32_t pos = base + (uint32_t)__popc(hm & ((1u << lane) - 1u));
-        if (pos < hit_cap) {
-          pps_hit h;
-          h.p = p;
-          h.k = k;
-          h.n = n + i;
-          h.idx = idx;
-          hits[pos] = h;
-        }
+// ---- queued 32-bit-step walk.  The hot loop only appends (lane, block) to a
+// per-warp queue in shared memory when a block of U steps is flagged; after the
+// warp's primes finish their walk, the warp re-checks the queued blocks together
+// (one block per lane), recomputing each block's starting value as
+// -/+2^-(nmin + 32 U b) mod p.  The hot loop thus holds no exact-check code.
+constexpr int WQ_CAP = 256;   // queue entries per warp
+constexpr int WQ_WARPS = 8;   // warps per 256-thread block
+
+__device__ __forceinline__ void record_exact(uint32_t klo, uint32_t khi, uint32_t n, uint64_t p, uint32_t idx,
+                                             uint64_t kmin, uint64_t kmax, uint32_t nmax, pps_hit* hits,
+                                             uint32_t* hit_count, uint32_t hit_cap) {
+  const uint32_t i = klo ? (uint32_t)(__ffs(klo) - 1) : (uint32_t)(31 + __ffs(khi));
+  const uint64_t k = mk64(klo, khi) >> (i & 63u);
+  const bool hit = (i < 32u) && (k <= kmax) && (k >= kmin) && (n + i < nmax);
+  const unsigned act = __activemask();
+  const unsigned hm = __ballot_sync(act, hit);
+  if (hm) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(hm) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(hit_count, (uint32_t)__popc(hm));
+    base = __shfl_sync(act, base, leader);
+    if (hit) {
+      const uint32_t pos = base + (uint32_t)__popc(hm & ((1u << lane) - 1u));
+      if (pos < hit_cap) {
+        pps_hit h;
+        h.p = p;
+        h.k = k;
+        h.n = n + i;
+        h.idx = idx;
+        hits[pos] = h;
       }
     }
-    step_chain32(klo, khi, plo, phi, pinv);
   }
 }
 
-// TEST 0: window via a running minimum (valid when win_hi == 0): a candidate has
-//         hi word 0 or low-word bits under win_mask all zero, so min(hi, lo & mask)
-//         is 0 at it; the block is flagged when the minimum over it is 0.
-// TEST 1: window, general form (hi <= win_hi or (lo & win_mask) == 0).
-// TEST 2: single bound (valid when p > kmax 2^43): a candidate K = k 2^i with i < 32
-//         has hi word <= floor(kmax 2^31 / 2^32) = win_hi.
-template <int TEST, int U>
-__global__ void __launch_bounds__(256, 8) k_walk32(WalkArgs a) {
+template <int TEST, int U, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
+  __shared__ uint32_t q_ent[WQ_WARPS][WQ_CAP];
+  __shared__ uint64_t q_p[WQ_WARPS][32];
+  __shared__ uint32_t q_cnt[WQ_WARPS];
   const uint64_t np = a.d_np ? *a.d_np : a.np;
   const uint32_t win_hi = a.win_hi, win_mask = a.win_mask, bound_hi = a.bound_hi;
   const uint32_t nsteps = a.nsteps, nmin = a.nmin;
-  const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t pi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pi < np; pi += gstride) {
-    const uint64_t p = a.P[pi];
-    const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
-    const uint64_t x = inv_pow2(nmin, p, ps);
-    const uint64_t K = a.proth ? p - x : x;
-    uint32_t klo = lo32(K), khi = hi32(K);
-    const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
-    uint32_t t = 0;
-    for (; t + U <= nsteps; t += U) {
-      const uint32_t slo = klo, shi = khi;
-      uint32_t acc = 0xffffffffu;
-      bool f = false;
+  const uint32_t full = nsteps / (uint32_t)U;  // whole blocks of U steps
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint64_t wstride = (uint64_t)gridDim.x * blockDim.x;
+  if (lane == 0) q_cnt[wib] = 0;
+  __syncwarp();
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < np;
+       base += wstride) {
+    const uint64_t pi = base + lane;
+    const bool valid = pi < np;
+    const uint64_t p = a.P[valid ? pi : base];
+    q_p[wib][lane] = p;
+    if (valid) {
+      const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
+      const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
+      const uint64_t x = inv_pow2(nmin, p, ps);
+      const uint64_t K = a.proth ? p - x : x;
+      uint32_t klo = lo32(K), khi = hi32(K);
+      for (uint32_t b = 0; b < full; ++b) {
+        uint32_t acc = 0xffffffffu;
+        bool f = false;
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (TEST == 0) acc = min(acc, min(khi, klo & win_mask));
-        else if (TEST == 1) f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
-        else f |= khi <= bound_hi;
+        for (int u = 0; u < U; ++u) {
+          if (TEST == 0) acc = min(acc, min(khi, klo & win_mask));
+          else if (TEST == 1) f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
+          else f |= khi <= bound_hi;
+          step_chain32(klo, khi, plo, phi, pinv);
+        }
+        if (TEST == 0) f = acc == 0u;
+        if (f) {
+          const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
+          if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | b;
+        }
+      }
+      // the last partial block (fewer than U steps) always goes to the queue
+      if (full * (uint32_t)U < nsteps) {
+        const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
+        if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | full;
+      }
+    }
+    __syncwarp();
+    const uint32_t cnt = q_cnt[wib];
+    if (cnt <= (uint32_t)WQ_CAP) {
+      // re-check the queued blocks exactly, one block per lane
+      for (uint32_t e = lane; e < cnt; e += 32u) {
+        const uint32_t ent = q_ent[wib][e];
+        const uint32_t owner = ent >> 27, blk = ent & ((1u << 27) - 1u);
+        const uint64_t op = q_p[wib][owner];
+        const uint64_t ops = neg_inv64(op);
+        const uint32_t t0 = (uint32_t)U * blk;
+        const uint32_t nblk = min((uint32_t)U, nsteps - t0);
+        const uint32_t n0 = nmin + 32u * t0;
+        const uint64_t x = inv_pow2(n0, op, ops);
+        const uint64_t K = a.proth ? op - x : x;
+        uint32_t klo = lo32(K), khi = hi32(K);
+        const uint32_t oplo = lo32(op), ophi = hi32(op), opinv = lo32(ops);
+#pragma unroll 1
+        for (uint32_t u = 0; u < nblk; ++u) {
+          record_exact(klo, khi, n0 + 32u * u, op, a.idx_base + (uint32_t)(base + owner), a.kmin, a.kmax,
+                       a.nmax, a.hits, a.hit_count, a.hit_cap);
+          step_chain32(klo, khi, oplo, ophi, opinv);
+        }
+      }
+    } else if (valid) {
+      // queue overflow (not expected at the designed false-pass rates): each
+      // lane re-walks its own prime with the exact test at every step
+      const uint64_t ps = neg_inv64(p);
+      const uint64_t x = inv_pow2(nmin, p, ps);
+      const uint64_t K = a.proth ? p - x : x;
+      uint32_t klo = lo32(K), khi = hi32(K);
+      const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
+#pragma unroll 1
+      for (uint32_t t = 0; t < nsteps; ++t) {
+        record_exact(klo, khi, nmin + 32u * t, p, a.idx_base + (uint32_t)pi, a.kmin, a.kmax, a.nmax,
+                     a.hits, a.hit_count, a.hit_cap);
         step_chain32(klo, khi, plo, phi, pinv);
       }
-      if (TEST == 0) f = acc == 0u;
-      if (f)
-        replay_block32(slo, shi, plo, phi, pinv, nmin + 32u * t, U, p, a.idx_base + (uint32_t)pi,
-                       a.kmin, a.kmax, a.nmax, a.hits, a.hit_count, a.hit_cap);
     }
-    if (t < nsteps)
-      replay_block32(klo, khi, plo, phi, pinv, nmin + 32u * t, nsteps - t, p,
-                     a.idx_base + (uint32_t)pi, a.kmin, a.kmax, a.nmax, a.hits, a.hit_count,
-                     a.hit_cap);
+    __syncwarp();
+    if (lane == 0) q_cnt[wib] = 0;
+    __syncwarp();
   }
 }
 
@@ -440,8 +489,9 @@ static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
     {"form0-window-u4-step"}, {"chain-window-u4-step"}, {"chain-window-u8-block"},
     {"form2-window-u8-block"}, {"form0-window-u8-block"}, {"chain-window-u8-block-ilp2"},
     {"form2-window-u8-block-ilp2"}, {"chain-lowbit-u8-block"}, {"form0-lowbit-u8-block"},
-    {"chain-window-u16-block"}, {"lean-min-u8"}, {"lean-window-u8"}, {"lean-bound-u8"},
-    {"lean-min-u16"}, {"lean-bound-u16"},
+    {"chain-window-u16-block"}, {"queue-min-u8"}, {"queue-window-u8"}, {"queue-bound-u8"},
+    {"queue-min-u16"}, {"queue-bound-u16"}, {"queue-min-u8-r40"}, {"queue-bound-u8-r40"},
+    {"queue-window-u8-r40"},
 };
 
 const char* walk_variant_name(int v) {
@@ -463,11 +513,14 @@ static walk_fn pick(int v) {
     case 7: return k_walk<1, 1, 8, S32, 1, true>;
     case 8: return k_walk<0, 1, 8, S32, 1, true>;
     case 9: return k_walk<1, 0, 16, S32, 1, true>;
-    case 10: return S32 ? k_walk32<0, 8> : nullptr;
-    case 11: return S32 ? k_walk32<1, 8> : nullptr;
-    case 12: return S32 ? k_walk32<2, 8> : nullptr;
-    case 13: return S32 ? k_walk32<0, 16> : nullptr;
-    case 14: return S32 ? k_walk32<2, 16> : nullptr;
+    case 10: return S32 ? k_walk32q<0, 8, 8> : nullptr;
+    case 11: return S32 ? k_walk32q<1, 8, 8> : nullptr;
+    case 12: return S32 ? k_walk32q<2, 8, 8> : nullptr;
+    case 13: return S32 ? k_walk32q<0, 16, 8> : nullptr;
+    case 14: return S32 ? k_walk32q<2, 16, 8> : nullptr;
+    case 15: return S32 ? k_walk32q<0, 8, 6> : nullptr;
+    case 16: return S32 ? k_walk32q<2, 8, 6> : nullptr;
+    case 17: return S32 ? k_walk32q<1, 8, 6> : nullptr;
   }
   return nullptr;
 }

@@ -53,7 +53,7 @@ def test_kat49_planted(pps, engine, kat49):
             assert want in got
 
 
-@pytest.mark.parametrize("variant", list(range(15)))
+@pytest.mark.parametrize("variant", list(range(18)))
 def test_every_walk_variant_matches_oracle(pps, engine, ora, variant):
     specs = [
         dict(pmin=10**12, pmax=10**12 + 3 * 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=5000),
