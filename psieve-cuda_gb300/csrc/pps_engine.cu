@@ -493,7 +493,8 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
     return e->forced_variant;
   if (e->tuned_variant[cls] >= 0 && variant_ok(jp, e->tuned_variant[cls])) return e->tuned_variant[cls];
   const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
-  const uint32_t cap_steps = 1024;
+  // long enough that per-prime setup does not dominate the comparison
+  const uint32_t cap_steps = 4096;
   int best = 0;
   float best_ms = 1e30f;
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
