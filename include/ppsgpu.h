@@ -165,6 +165,26 @@ int pps_measure_imad_peak(pps_engine *e, double *mults_per_sec);
 /* Number of the engine's own kernels launched so far. */
 uint64_t pps_engine_launches(const pps_engine *e);
 
+/* Allocation-free walk (no counterpart in the reference): the walk and the
+   output rule over np primes already in device memory (d_P), factors written
+   to the caller's device buffer d_out (capacity out_cap, in no particular
+   order), their count to *nout (host).  For callers that cannot call
+   cudaMalloc -- device memory owned by another allocator or pool, or code that
+   must not allocate while it runs: this call allocates nothing; its candidate
+   scratch is a fixed __device__ array that each GPU loading the library holds
+   until exit.  Limits: np <= PPS_NOALLOC_MAX_PRIMES per call (larger lists are
+   rejected with PPS_ERR_INVALID_PARAM), and at most PPS_NOALLOC_MAX_CANDIDATES
+   raw candidates per call (beyond that PPS_ERR_OVERFLOW: split the list).
+   stream: a cudaStream_t or NULL; the call returns after the work finished.
+   The first call on a device sets the scratch up (make it before any stream
+   capture).  All calls on a device share the scratch: calls that overlap on
+   the GPU race, so serialise them.  Errors: pps_last_error(). */
+#define PPS_NOALLOC_MAX_PRIMES (1u << 24)
+#define PPS_NOALLOC_MAX_CANDIDATES (1u << 16)
+int pps_check_primes_noalloc(const pps_job_params *jp, const uint64_t *d_P, size_t np,
+                             pps_factor *d_out, uint32_t out_cap, uint32_t *nout,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{CSRC}"]
 
-LIB_SOURCES = ["pps_kernels.cu", "pps_engine.cu", "pps_batch.cu", "pps_server.cu"]
+LIB_SOURCES = ["pps_kernels.cu", "pps_engine.cu", "pps_batch.cu", "pps_server.cu",
+               "pps_noalloc.cu"]
 COMPAT_SOURCES = ["appcu_compat.cu"]
 
 

@@ -482,6 +482,12 @@ static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64
   return PPS_OK;
 }
 
+namespace pps {
+void walk_args_for_job(const pps_job_params* jp, WalkArgs* a) { fill_walk_args(jp, a); }
+int walk_variant_exact(const pps_job_params* jp, int v) { return variant_ok(jp, v); }
+int set_error_text(int code, const char* msg) { return set_err(code, "%s", msg); }
+}  // namespace pps
+
 // Time each walk variant on the first `np` resident primes with a capped n
 // range and keep the fastest for this step class.
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,

@@ -61,6 +61,12 @@ struct WalkArgs {
 
 // Variant v in [0, PPS_NUM_VARIANTS): step formulation x pre-test x unroll.
 const char* walk_variant_name(int v);
+// Pre-test constants of a normalised job, and whether variant v is exact for it
+// (defined in pps_engine.cu).
+void walk_args_for_job(const pps_job_params* jp, WalkArgs* a);
+int walk_variant_exact(const pps_job_params* jp, int v);
+// Record an error message for pps_last_error(); returns code.
+int set_error_text(int code, const char* msg);
 // Largest useful grid for the walk kernel of variant v with `threads` threads
 // per block (occupancy-derived); 0 if the variant cannot run this step size.
 int walk_max_blocks(int v, int threads, uint32_t step, int num_sms);

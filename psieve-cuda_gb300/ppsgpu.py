@@ -112,6 +112,9 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_sieve_range": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                                            ctypes.c_uint32, u64p, ctypes.c_size_t, szp, u64p]),
         "pps_measure_imad_peak": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_double)]),
+        "pps_check_primes_noalloc": (ctypes.c_int, [P(JobParams), ctypes.c_void_p, ctypes.c_size_t,
+                                                    ctypes.c_void_p, ctypes.c_uint32,
+                                                    P(ctypes.c_uint32), ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
