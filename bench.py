@@ -153,6 +153,42 @@ def cpu_sample(seconds_target: float = 10.0, nthreads: int | None = None) -> dic
             "n_steps_per_sec": count * steps / dt, "seconds": dt, "primes": count}
 
 
+def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
+    """Configuration 4: `count` heterogeneous jobs from `seed`, as plain one-job
+    runs (pps_run_job each) and as one batched persistent run (pps_run_batch);
+    the per-job results must be identical."""
+    import numpy as np
+
+    import ppsgpu
+
+    jobs, meta = ppsgpu.mixed_jobs(seed=seed, count=count)
+    repaired = sum(1 for m in meta if m[1])
+    # warm-up of both forms (kernel tuning for both step classes, graph capture)
+    warm = [j for j in jobs if j.step == 32][:2] + [j for j in jobs if j.step < 32][:2]
+    for jp in warm:
+        eng.run_job(jp)
+    eng.run_batch(jobs[: min(len(jobs), 64)])
+    t0 = time.perf_counter()
+    plain, plain_primes = [], 0
+    for jp in jobs:
+        fac, st = eng.run_job(jp)
+        plain.append(fac)
+        plain_primes += st.primes
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    per, bst = eng.run_batch(jobs)
+    t_batch = time.perf_counter() - t0
+    identical = len(per) == len(plain) and all(np.array_equal(a, b) for a, b in zip(per, plain))
+    return {"workload": f"{count} mixed jobs, seed {seed} (config 4 distribution); {repaired} "
+                        "jobs had pmin raised to meet the reference's 2^(64-nstep) <= pmin rule",
+            "primes": int(bst.primes), "steps": int(bst.steps), "factors": int(bst.factors),
+            "plain_s": t_plain, "batched_s": t_batch,
+            "plain_primes_per_s": plain_primes / t_plain, "batched_primes_per_s": bst.primes / t_batch,
+            "speedup": t_plain / t_batch, "identical_results": bool(identical),
+            "waves": int(bst.waves), "chunk": int(bst.chunk), "unroll": int(bst.unroll),
+            "batched_n_steps_per_s": bst.steps / t_batch}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = _dist()
     if rank != 0:
@@ -302,6 +338,7 @@ def run_gpu(args) -> None:
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                           "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
     cpu = None if args.no_cpu else cpu_sample(args.ref_seconds)
+    batched = None if args.no_batched else run_mixed(eng, args.mixed_jobs)
     line = {"metric": METRIC, "value": value, "unit": "primes/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -314,7 +351,8 @@ def run_gpu(args) -> None:
             "phase_ms": {"sieve": sieve_ms, "walk": walk_ms,
                          "filter": sum(s.filter_ms for s in stats)},
             "factors": sum(s.factors for s in stats),
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "batched": batched}
     print(json.dumps(line), flush=True)
     eng.close()
     if ws > 1:
@@ -371,6 +409,8 @@ def main() -> None:
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--mixed-jobs", type=int, default=512)
     ap.add_argument("--profile", type=int, nargs=2, metavar=("SPAN", "NWIDTH"))
     ap.add_argument("--profile-reps", type=int, default=1)
     ap.add_argument("--variant", type=int, default=5)

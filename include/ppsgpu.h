@@ -165,6 +165,26 @@ int pps_measure_imad_peak(pps_engine *e, double *mults_per_sec);
 /* Number of the engine's own kernels launched so far. */
 uint64_t pps_engine_launches(const pps_engine *e);
 
+/* ---- Batched persistent form (no single counterpart in the reference, which
+   runs one range per process, main.c:887-1266).  Many normalised jobs --
+   different k, n and p ranges, mixed signs -- are sieved wave by wave into one
+   device prime table and walked by one persistent kernel whose warps take
+   chunks of primes from a device work counter; each wave's launch sequence is
+   a captured CUDA graph; the chunk size and unroll are tuned on the first
+   wave.  Factors come back grouped by job (job_offsets[j]..job_offsets[j+1]),
+   each group sorted by (p, k, n), exactly as pps_run_job would return them. */
+typedef struct {
+  uint64_t primes, prime_sum, raw_hits, factors, steps;
+  uint32_t waves, chunk, unroll, pad;
+  double total_ms, filter_ms;
+} pps_batch_stats;
+
+int pps_run_batch(pps_engine *e, const pps_job_params *jobs, size_t njobs, pps_factor *out,
+                  size_t cap, size_t *nout, size_t *job_offsets, pps_batch_stats *st);
+
+/* Per-job prime count and wrapping prime sum of the last pps_run_batch. */
+int pps_batch_job_primes(pps_engine *e, size_t njobs, uint64_t *primes, uint64_t *sums);
+
 /* Allocation-free walk (no counterpart in the reference): the walk and the
    output rule over np primes already in device memory (d_P), factors written
    to the caller's device buffer d_out (capacity out_cap, in no particular

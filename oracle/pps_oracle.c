@@ -464,8 +464,13 @@ long ppo_run(const ppo_params *pp, int nthreads, ppo_factor *out, size_t cap,
   memset(&j, 0, sizeof j);
   pthread_mutex_init(&j.mu, NULL);
   j.pp = pp; j.bp = &bp; j.out = out; j.cap = out ? cap : 0;
-  j.chunk = (uint64_t)1 << 22;
-  j.nchunks = (pp->pmax - pp->pmin + j.chunk - 1) / j.chunk;
+  /* at least ~8 chunks per thread, between 2^14 and 2^22 wide (even) */
+  uint64_t span = pp->pmax - pp->pmin;
+  uint64_t ch = span / ((uint64_t)(nthreads > 0 ? nthreads : 1) * 8);
+  if (ch < ((uint64_t)1 << 14)) ch = (uint64_t)1 << 14;
+  if (ch > ((uint64_t)1 << 22)) ch = (uint64_t)1 << 22;
+  j.chunk = ch & ~(uint64_t)1;
+  j.nchunks = (span + j.chunk - 1) / j.chunk;
   long r = run_threads(&j, range_worker, nthreads);
   if (count) *count = j.count;
   if (sum) *sum = j.sum;

@@ -1,0 +1,828 @@
+// pps_batch.cu -- the batched persistent form: many uneven jobs (different k,
+// n and p ranges, mixed +/- sides) in one persistent walk kernel fed by a
+// device work queue.
+//
+// A job's p range is cut into batches (contiguous sieve segments of 2^18 odd
+// candidates).  Batches of many jobs fill a wave (up to WAVE_SEGS segments).
+// Per wave, one fixed launch sequence -- large-prime scatter, segment sieve,
+// scan, expansion, chunking, scan, persistent walk -- reads every count from
+// device tables, so it is captured once as a CUDA graph and replayed for each
+// wave after the wave's tables are copied in.  The walk kernel's warps pop
+// chunks of CHUNK primes (all of one job, so every lane of a warp has the same
+// n loop) from a device counter until the wave is exhausted.  Raw candidates
+// carry their job id; one filter launch after the last wave applies each
+// job's output rule.
+//
+// Reference counterpart: none in one piece -- the reference runs one range per
+// process (main.c:887-1266) and one kernel per n slice (pps/appcu.cu:1194-1261).
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "pps_device.cuh"
+#include "pps_engine_impl.h"
+
+namespace pps {
+
+constexpr uint32_t WAVE_SEGS = 1u << 14;        // segments per wave (2^32 odd candidates)
+constexpr uint32_t BATCH_SEGS = 1u << 12;       // segments per batch
+constexpr uint32_t WAVE_BATCHES = WAVE_SEGS;    // at most one batch per segment
+constexpr uint32_t MAX_JOBS = 1u << 16;
+constexpr int BW_THREADS = 256;
+constexpr uint32_t BQ_CAP = 256;  // queued blocks per warp
+
+struct BJob {
+  uint64_t kmin, kmax, kstep, koffset;
+  uint32_t nmin, nmax, step, nsteps;
+  uint32_t proth, win_hi, win_mask, qmax;
+  int32_t sign;
+  uint32_t pad;
+};
+
+struct BBatch {
+  uint64_t lo, nbits;
+  uint32_t seg0, job;
+  uint32_t nq, nq_tiny, nq_seg, limit;  // limit = largest sieving prime allowed
+};
+
+struct BSeg {
+  uint64_t lo;
+  uint32_t bits, batch;
+};
+
+struct WaveTables {  // pinned host staging == device layout
+  uint32_t nseg, nbatch, pad0, pad1;
+  BSeg seg[WAVE_SEGS];
+  BBatch batch[WAVE_BATCHES];
+};
+
+}  // namespace pps
+
+using namespace pps;
+
+struct BatchState {
+  bool ready = false;
+  DevBuf<uint8_t> tables;       // WaveTables
+  WaveTables* h_tables = nullptr;
+  DevBuf<BJob> jobs;
+  DevBuf<uint32_t> bitmap;      // WAVE_SEGS * SEG_WORDS
+  DevBuf<uint32_t> seg_count, seg_off, chunk_count, chunk_off;
+  DevBuf<uint64_t> P, Pinv;
+  DevBuf<uint64_t> tot;         // [0] primes, [1] sum, [2] chunks, [3] work counter
+  DevBuf<unsigned long long> job_primes, job_sum;
+  DevBuf<pps_hit> hits, out;
+  DevBuf<uint32_t> counters;    // [0] raw, [1] survivors
+  uint64_t prime_cap = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_chunk = 0, graph_unroll = 0;
+  cudaEvent_t copied = nullptr;
+  int tuned_chunk = 0, tuned_unroll = 0;
+};
+
+void batch_state_free(pps_engine* e) {
+  BatchState* b = e->batch;
+  if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->copied) cudaEventDestroy(b->copied);
+  if (b->h_tables) cudaFreeHost(b->h_tables);
+  b->tables.release();
+  b->jobs.release();
+  b->bitmap.release();
+  b->seg_count.release();
+  b->seg_off.release();
+  b->chunk_count.release();
+  b->chunk_off.release();
+  b->P.release();
+  b->Pinv.release();
+  b->tot.release();
+  b->job_primes.release();
+  b->job_sum.release();
+  b->hits.release();
+  b->out.release();
+  b->counters.release();
+  delete b;
+  e->batch = nullptr;
+}
+
+namespace pps {
+
+__device__ __forceinline__ const WaveTables* wt(const uint8_t* t) { return (const WaveTables*)t; }
+
+// per batch: how many of the ascending sieving primes are <= its limit
+__global__ void k_bcounts(uint8_t* tables, const uint32_t* q, uint32_t nq_all) {
+  WaveTables* T = (WaveTables*)tables;
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < T->nbatch; b += gridDim.x * blockDim.x) {
+    BBatch& B = T->batch[b];
+    uint32_t lo = 0, hi = nq_all;
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if (q[mid] <= B.limit) lo = mid + 1; else hi = mid;
+    }
+    B.nq = lo;
+    uint32_t t = 0, s = 0;
+    {
+      uint32_t l2 = 0, h2 = lo;
+      while (l2 < h2) {
+        const uint32_t mid = l2 + (h2 - l2) / 2;
+        if (q[mid] < TINY_Q_LIMIT) l2 = mid + 1; else h2 = mid;
+      }
+      t = l2;
+      l2 = 0;
+      h2 = lo;
+      while (l2 < h2) {
+        const uint32_t mid = l2 + (h2 - l2) / 2;
+        if (q[mid] < SEG_BITS) l2 = mid + 1; else h2 = mid;
+      }
+      s = l2;
+    }
+    B.nq_tiny = t;
+    B.nq_seg = s;
+  }
+}
+
+__device__ __forceinline__ uint64_t b_first_odd_multiple(uint64_t q, uint64_t lo) {
+  uint64_t st = q * q;
+  if (st < lo) {
+    const uint64_t r = lo % q;
+    st = r ? lo + (q - r) : lo;
+    if ((st & 1ull) == 0ull) st += q;
+  }
+  return st;
+}
+
+// large sieving primes of batch blockIdx.y into the wave bitmap
+__global__ void k_bsieve_large(const uint8_t* tables, const uint32_t* q, uint32_t* bitmap) {
+  const WaveTables* T = wt(tables);
+  const uint32_t b = blockIdx.y;
+  if (b >= T->nbatch) return;
+  const BBatch B = T->batch[b];
+  if (B.nq <= B.nq_seg) return;
+  uint32_t* bm = bitmap + (size_t)B.seg0 * SEG_WORDS;
+  const uint64_t hi = B.lo + 2ull * B.nbits;
+  for (uint32_t i = B.nq_seg + blockIdx.x * blockDim.x + threadIdx.x; i < B.nq; i += gridDim.x * blockDim.x) {
+    const uint64_t qq = q[i];
+    if (qq * qq >= hi) continue;
+    const uint64_t st = b_first_odd_multiple(qq, B.lo);
+    for (uint64_t j = (st - B.lo) >> 1; j < B.nbits; j += qq) atomicAnd(&bm[j >> 5], ~(1u << (j & 31u)));
+  }
+}
+
+__global__ void __launch_bounds__(SIEVE_THREADS) k_bsieve_seg(const uint8_t* tables, const uint32_t* q,
+                                                              uint32_t* bitmap, uint32_t* seg_count) {
+  __shared__ uint32_t sb[SEG_WORDS];
+  __shared__ uint32_t warp_cnt[SIEVE_THREADS / 32];
+  const WaveTables* T = wt(tables);
+  const uint32_t seg = blockIdx.x;
+  if (seg >= T->nseg) {
+    if (threadIdx.x == 0) seg_count[seg] = 0;
+    return;
+  }
+  const BSeg S = T->seg[seg];
+  const BBatch B = T->batch[S.batch];
+  const uint32_t bits = S.bits;
+  const uint64_t seg_lo = S.lo, seg_hi = seg_lo + 2ull * bits;
+  const int have_large = B.nq > B.nq_seg;
+  uint32_t* gw = bitmap + (size_t)seg * SEG_WORDS;
+  for (uint32_t w = threadIdx.x; w < SEG_WORDS; w += blockDim.x) {
+    uint32_t v = have_large ? gw[w] : 0xffffffffu;
+    const uint32_t j0 = w * 32u;
+    if (j0 >= bits) v = 0u;
+    else if (bits - j0 < 32u) v &= (1u << (bits - j0)) - 1u;
+    sb[w] = v;
+  }
+  __syncthreads();
+  for (uint32_t i = 0; i < B.nq_tiny; ++i) {
+    const uint64_t qq = q[i];
+    if (qq * qq >= seg_hi) break;
+    const uint64_t st = b_first_odd_multiple(qq, seg_lo);
+    for (uint64_t j = ((st - seg_lo) >> 1) + (uint64_t)threadIdx.x * qq; j < bits; j += (uint64_t)blockDim.x * qq)
+      atomicAnd(&sb[j >> 5], ~(1u << (j & 31u)));
+  }
+  const uint32_t qend = B.nq_seg < B.nq ? B.nq_seg : B.nq;
+  for (uint32_t i = B.nq_tiny + threadIdx.x; i < qend; i += blockDim.x) {
+    const uint64_t qq = q[i];
+    if (qq * qq >= seg_hi) continue;
+    const uint64_t st = b_first_odd_multiple(qq, seg_lo);
+    for (uint64_t j = (st - seg_lo) >> 1; j < bits; j += (uint32_t)qq) atomicAnd(&sb[j >> 5], ~(1u << (j & 31u)));
+  }
+  __syncthreads();
+  uint32_t cnt = 0;
+  for (uint32_t w = threadIdx.x; w < SEG_WORDS; w += blockDim.x) {
+    const uint32_t v = sb[w];
+    gw[w] = v;
+    cnt += __popc(v);
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += warp_cnt[i];
+    seg_count[seg] = t;
+  }
+}
+
+// exclusive scan of n counts (one CTA); total into *total
+__global__ void __launch_bounds__(1024) k_bscan(const uint32_t* cnt, uint32_t* off, uint32_t n, uint64_t* total) {
+  __shared__ uint64_t part[1024];
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t a = threadIdx.x * per;
+  const uint32_t e = a + per < n ? a + per : n;
+  uint64_t s = 0;
+  for (uint32_t i = a; i < e; ++i) s += cnt[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t d = 1; d < blockDim.x; d <<= 1) {
+    const uint64_t v = threadIdx.x >= d ? part[threadIdx.x - d] : 0ull;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint64_t run = part[threadIdx.x] - s;
+  for (uint32_t i = a; i < e; ++i) {
+    off[i] = (uint32_t)run;
+    run += cnt[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) *total = part[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(SIEVE_THREADS) k_bexpand(const uint8_t* tables, const uint32_t* bitmap,
+                                                           const uint32_t* seg_off, uint64_t* P, uint64_t* Pinv,
+                                                           unsigned long long* job_primes,
+                                                           unsigned long long* job_sum, uint64_t cap) {
+  constexpr uint32_t WPT = SEG_WORDS / SIEVE_THREADS;
+  __shared__ uint32_t warp_tot[SIEVE_THREADS / 32];
+  __shared__ unsigned long long blk_sum;
+  const WaveTables* T = wt(tables);
+  const uint32_t seg = blockIdx.x;
+  if (seg >= T->nseg) return;
+  const BSeg S = T->seg[seg];
+  const uint32_t job = T->batch[S.batch].job;
+  const uint32_t* gw = bitmap + (size_t)seg * SEG_WORDS + threadIdx.x * WPT;
+  const uint64_t base_val = S.lo + 2ull * (threadIdx.x * WPT * 32u);
+  uint32_t w[WPT];
+  uint32_t c = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < WPT; ++i) {
+    w[i] = gw[i];
+    c += __popc(w[i]);
+  }
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  uint32_t inc = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc += v;
+  }
+  if (lane == 31) warp_tot[wid] = inc;
+  if (threadIdx.x == 0) blk_sum = 0ull;
+  __syncthreads();
+  uint32_t woff = 0;
+  for (uint32_t i = 0; i < wid; ++i) woff += warp_tot[i];
+  uint64_t pos = (uint64_t)seg_off[seg] + woff + inc - c;
+  uint64_t sum = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < WPT; ++i) {
+    uint32_t v = w[i];
+    while (v) {
+      const uint32_t bit = __ffs(v) - 1u;
+      v &= v - 1u;
+      const uint64_t p = base_val + 2ull * (i * 32u + bit);
+      sum += p;
+      if (pos < cap) {
+        P[pos] = p;
+        Pinv[pos] = neg_inv64(p);
+      }
+      ++pos;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  if (lane == 0) atomicAdd(&blk_sum, (unsigned long long)sum);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (uint32_t i = 0; i < (SIEVE_THREADS >> 5); ++i) tot += warp_tot[i];
+    atomicAdd(&job_primes[job], (unsigned long long)tot);
+    atomicAdd(&job_sum[job], blk_sum);
+  }
+}
+
+__global__ void k_bchunks(const uint8_t* tables, const uint32_t* seg_count, uint32_t* chunk_count,
+                          uint32_t chunk) {
+  const WaveTables* T = wt(tables);
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < WAVE_SEGS; s += gridDim.x * blockDim.x)
+    chunk_count[s] = s < T->nseg ? (seg_count[s] + chunk - 1) / chunk : 0u;
+}
+
+__device__ __forceinline__ void b_record(uint32_t klo, uint32_t khi, uint32_t n, uint32_t step, uint64_t p,
+                                         uint32_t job, const BJob& J, pps_hit* hits, uint32_t* hit_count,
+                                         uint32_t hit_cap) {
+  const uint32_t i = klo ? (uint32_t)(__ffs(klo) - 1) : (uint32_t)(31 + __ffs(khi));
+  const uint64_t k = mk64(klo, khi) >> (i & 63u);
+  const bool hit = (i < step) && (k <= J.kmax) && (k >= J.kmin) && (n + i < J.nmax);
+  const unsigned act = __activemask();
+  const unsigned hm = __ballot_sync(act, hit);
+  if (hm) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(hm) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(hit_count, (uint32_t)__popc(hm));
+    base = __shfl_sync(act, base, leader);
+    if (hit) {
+      const uint32_t pos = base + (uint32_t)__popc(hm & ((1u << lane) - 1u));
+      if (pos < hit_cap) {
+        pps_hit h;
+        h.p = p;
+        h.k = k;
+        h.n = n + i;
+        h.idx = job;
+        hits[pos] = h;
+      }
+    }
+  }
+}
+
+template <bool S32>
+__device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi, uint32_t pinv_s,
+                                       uint32_t s) {
+  if (S32) step_chain32(klo, khi, plo, phi, pinv_s);
+  else step_form0<false>(klo, khi, plo, phi, pinv_s, s);
+}
+
+// One round: every lane walks one prime of the same job; flagged blocks of U
+// steps (and the partial last block) go to the warp's queue and are re-checked
+// exactly once the round's walks are done.
+template <bool S32, int U>
+__device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
+                                        uint32_t* qe, uint32_t* qc, uint64_t* qp, pps_hit* hits,
+                                        uint32_t* hit_count, uint32_t hit_cap) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t s = S32 ? 32u : J.step;
+  const uint32_t nsteps = J.nsteps, full = nsteps / (uint32_t)U;
+  qp[lane] = p;
+  if (valid) {
+    const uint32_t plo = lo32(p), phi = hi32(p);
+    const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
+    const uint64_t x = inv_pow2(J.nmin, p, ps);
+    const uint64_t K = J.proth ? p - x : x;
+    uint32_t klo = lo32(K), khi = hi32(K);
+    const uint32_t win_hi = J.win_hi, win_mask = J.win_mask;
+    for (uint32_t b = 0; b < full; ++b) {
+      bool f = false;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
+        b_step<S32>(klo, khi, plo, phi, pinv_s, s);
+      }
+      if (f) {
+        const uint32_t pos = atomicAdd(qc, 1u);
+        if (pos < BQ_CAP) qe[pos] = (lane << 27) | b;
+      }
+    }
+    if (full * (uint32_t)U < nsteps) {
+      const uint32_t pos = atomicAdd(qc, 1u);
+      if (pos < BQ_CAP) qe[pos] = (lane << 27) | full;
+    }
+  }
+  __syncwarp();
+  const uint32_t cnt = *qc;
+  if (cnt <= BQ_CAP) {
+    for (uint32_t e = lane; e < cnt; e += 32u) {
+      const uint32_t ent = qe[e];
+      const uint32_t owner = ent >> 27, blk = ent & ((1u << 27) - 1u);
+      const uint64_t op = qp[owner];
+      const uint64_t ops = neg_inv64(op);
+      const uint32_t t0 = (uint32_t)U * blk;
+      const uint32_t nblk = min((uint32_t)U, nsteps - t0);
+      const uint32_t n0 = J.nmin + s * t0;
+      const uint64_t x = inv_pow2(n0, op, ops);
+      const uint64_t K = J.proth ? op - x : x;
+      uint32_t klo = lo32(K), khi = hi32(K);
+      const uint32_t oplo = lo32(op), ophi = hi32(op);
+      const uint32_t opinv = S32 ? lo32(ops) : (lo32(ops) << (32u - s));
+#pragma unroll 1
+      for (uint32_t u = 0; u < nblk; ++u) {
+        b_record(klo, khi, n0 + s * u, s, op, job, J, hits, hit_count, hit_cap);
+        b_step<S32>(klo, khi, oplo, ophi, opinv, s);
+      }
+    }
+  } else if (valid) {
+    const uint32_t plo = lo32(p), phi = hi32(p);
+    const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
+    const uint64_t x = inv_pow2(J.nmin, p, ps);
+    const uint64_t K = J.proth ? p - x : x;
+    uint32_t klo = lo32(K), khi = hi32(K);
+#pragma unroll 1
+    for (uint32_t t = 0; t < nsteps; ++t) {
+      b_record(klo, khi, J.nmin + s * t, s, p, job, J, hits, hit_count, hit_cap);
+      b_step<S32>(klo, khi, plo, phi, pinv_s, s);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) *qc = 0;
+  __syncwarp();
+}
+
+template <int U>
+__global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, const BJob* jobs,
+                                                         const uint32_t* seg_count, const uint32_t* seg_off,
+                                                         const uint32_t* chunk_off, const uint64_t* P,
+                                                         const uint64_t* Pinv, uint64_t* tot, uint32_t chunk,
+                                                         uint64_t chunk_limit, pps_hit* hits,
+                                                         uint32_t* hit_count, uint32_t hit_cap) {
+  __shared__ uint32_t q_ent[BW_THREADS / 32][BQ_CAP];
+  __shared__ uint64_t q_p[BW_THREADS / 32][32];
+  __shared__ uint32_t q_cnt[BW_THREADS / 32];
+  const WaveTables* T = wt(tables);
+  const uint32_t nseg = T->nseg;
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  uint64_t nchunks = tot[2];
+  if (chunk_limit && chunk_limit < nchunks) nchunks = chunk_limit;
+  if (lane == 0) q_cnt[wib] = 0;
+  __syncwarp();
+  for (;;) {
+    uint64_t c = 0;
+    if (lane == 0) c = atomicAdd((unsigned long long*)&tot[3], 1ull);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= nchunks) break;
+    // segment of chunk c: last s with chunk_off[s] <= c
+    uint32_t lo = 0, hi = nseg;
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if ((uint64_t)chunk_off[mid] <= c) lo = mid + 1; else hi = mid;
+    }
+    const uint32_t s = lo - 1;
+    const uint32_t job = T->batch[T->seg[s].batch].job;
+    const BJob J = jobs[job];
+    const uint32_t within = (uint32_t)(c - chunk_off[s]) * chunk;
+    const uint32_t count = min(chunk, seg_count[s] - within);
+    const uint64_t first = (uint64_t)seg_off[s] + within;
+    for (uint32_t r = 0; r < count; r += 32u) {
+      const bool valid = r + lane < count;
+      const uint64_t pi = first + r + (valid ? lane : 0u);
+      const uint64_t p = P[pi], ps = Pinv[pi];
+      if (J.step == 32)
+        b_round<true, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], hits, hit_count, hit_cap);
+      else
+        b_round<false, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], hits, hit_count, hit_cap);
+    }
+  }
+}
+
+// output rule per candidate with its job's parameters
+__global__ void k_bfilter(const pps_hit* hits, const uint32_t* d_nhits, uint32_t hit_cap, const BJob* jobs,
+                          const uint16_t* small_q, uint32_t nsmall, pps_hit* out, uint32_t* out_count,
+                          uint32_t out_cap) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  uint32_t nh = *d_nhits;
+  if (nh > hit_cap) nh = hit_cap;
+  for (uint32_t h = warp; h < nh; h += nwarps) {
+    const pps_hit x = hits[h];
+    const BJob J = jobs[x.idx];
+    bool ok = (x.k == J.kstep * (x.k / J.kstep) + J.koffset) && x.n >= J.nmin && x.n < J.nmax;
+    if (ok) {
+      bool div = false;
+      for (uint32_t base = 0; base < nsmall; base += 32u) {
+        const uint32_t i = base + lane;
+        if (i < nsmall) {
+          const uint32_t q = small_q[i];
+          const uint32_t kr = (uint32_t)(x.k % q);
+          uint32_t r = 1u, b = 2u % q, e = x.n;
+          while (e) {
+            if (e & 1u) r = (r * b) % q;
+            b = (b * b) % q;
+            e >>= 1;
+          }
+          const uint32_t t = (kr * r) % q;
+          div = ((t + (uint32_t)((int32_t)q + J.sign)) % q) == 0u;
+        }
+        if (__any_sync(0xffffffffu, div)) break;
+      }
+      ok = !__any_sync(0xffffffffu, div);
+    }
+    if (ok && lane == 0) {
+      const uint32_t pos = atomicAdd(out_count, 1u);
+      if (pos < out_cap) out[pos] = x;
+    }
+  }
+}
+
+}  // namespace pps
+
+// --------------------------------------------------------------- host side
+
+namespace {
+
+struct BatchPlan {
+  std::vector<BBatch> batches;  // in wave order
+};
+
+int ensure_state(pps_engine* e, size_t njobs) {
+  if (!e->batch) e->batch = new BatchState();
+  BatchState* b = e->batch;
+  int rc;
+  if (!b->ready) {
+    if ((rc = b->tables.ensure(sizeof(WaveTables)))) return rc;
+    if (cudaMallocHost(&b->h_tables, sizeof(WaveTables)) != cudaSuccess)
+      return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "pinned table staging");
+    if ((rc = b->bitmap.ensure((size_t)WAVE_SEGS * SEG_WORDS))) return rc;
+    if ((rc = b->seg_count.ensure(WAVE_SEGS)) || (rc = b->seg_off.ensure(WAVE_SEGS)) ||
+        (rc = b->chunk_count.ensure(WAVE_SEGS)) || (rc = b->chunk_off.ensure(WAVE_SEGS)))
+      return rc;
+    // p > 2^32: odd primes are fewer than 1/10 of the odd candidates
+    b->prime_cap = (uint64_t)WAVE_SEGS * SEG_BITS / 10 + 4096;
+    if ((rc = b->P.ensure(b->prime_cap)) || (rc = b->Pinv.ensure(b->prime_cap))) return rc;
+    if ((rc = b->tot.ensure(4))) return rc;
+    if ((rc = b->counters.ensure(4))) return rc;
+    if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
+    if (cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming) != cudaSuccess)
+      return set_err(PPS_ERR_CUDA, "event");
+    b->ready = true;
+  }
+  if ((rc = b->jobs.ensure(njobs)) || (rc = b->job_primes.ensure(njobs)) || (rc = b->job_sum.ensure(njobs)))
+    return rc;
+  return PPS_OK;
+}
+
+// The fixed per-wave launch sequence (everything reads counts from the tables).
+int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int chunk, int unroll, uint64_t chunk_limit,
+                pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
+  BatchState* b = e->batch;
+  cudaStream_t st = e->st;
+  CU(cudaMemsetAsync(b->bitmap.p, 0xff, (size_t)WAVE_SEGS * SEG_WORDS * 4, st));
+  CU(cudaMemsetAsync(b->tot.p, 0, 4 * sizeof(uint64_t), st));
+  k_bcounts<<<(WAVE_BATCHES + 255) / 256, 256, 0, st>>>(b->tables.p, dq, nq_all);
+  k_bsieve_large<<<dim3(8, WAVE_BATCHES), 256, 0, st>>>(b->tables.p, dq, b->bitmap.p);
+  k_bsieve_seg<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, dq, b->bitmap.p, b->seg_count.p);
+  k_bscan<<<1, 1024, 0, st>>>(b->seg_count.p, b->seg_off.p, WAVE_SEGS, b->tot.p);
+  k_bexpand<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, b->bitmap.p, b->seg_off.p, b->P.p, b->Pinv.p,
+                                                  b->job_primes.p, b->job_sum.p, b->prime_cap);
+  k_bchunks<<<(WAVE_SEGS + 255) / 256, 256, 0, st>>>(b->tables.p, b->seg_count.p, b->chunk_count.p, chunk);
+  k_bscan<<<1, 1024, 0, st>>>(b->chunk_count.p, b->chunk_off.p, WAVE_SEGS, b->tot.p + 2);
+  int per_sm = 0;
+  auto fn = unroll == 16 ? k_bwalk<16> : k_bwalk<8>;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
+  const int grid = (per_sm > 0 ? per_sm : 1) * e->num_sms;
+  fn<<<grid, BW_THREADS, 0, st>>>(b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->P.p,
+                                  b->Pinv.p, b->tot.p, (uint32_t)chunk, chunk_limit, hits, hit_count, hit_cap);
+  CU(cudaGetLastError());
+  e->launches += 9;
+  return PPS_OK;
+}
+
+}  // namespace
+
+extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t njobs, pps_factor* out,
+                             size_t cap, size_t* nout, size_t* job_offsets, pps_batch_stats* bst) {
+  if (!e || (!jobs && njobs)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  if (njobs > MAX_JOBS) return set_err(PPS_ERR_INVALID_PARAM, "at most %u jobs per batch", MAX_JOBS);
+  for (size_t j = 0; j < njobs; ++j)
+    if (jobs[j].step < 1 || jobs[j].step > 32 || jobs[j].pmin <= (1ull << 32))
+      return set_err(PPS_ERR_INVALID_PARAM, "job %zu not normalized", j);
+  CU(cudaSetDevice(e->device));
+  int rc;
+  if ((rc = ensure_state(e, njobs ? njobs : 1))) return rc;
+  BatchState* b = e->batch;
+  if (bst) memset(bst, 0, sizeof *bst);
+  CU(cudaEventRecord(e->ev[6], e->st));
+
+  // job table and the sieving-prime table for the largest p of the batch
+  std::vector<BJob> hj(njobs);
+  uint64_t pmax_all = 5;
+  uint32_t qmax_all = 3;
+  for (size_t j = 0; j < njobs; ++j) {
+    const pps_job_params& jp = jobs[j];
+    WalkArgs a;
+    walk_args_for_job(&jp, &a);
+    BJob& J = hj[j];
+    J.kmin = jp.kmin;
+    J.kmax = jp.kmax;
+    J.kstep = jp.kstep;
+    J.koffset = jp.koffset;
+    J.nmin = jp.nmin;
+    J.nmax = jp.nmax;
+    J.step = jp.step;
+    J.nsteps = a.nsteps;
+    J.proth = a.proth;
+    J.win_hi = a.win_hi;
+    J.win_mask = a.win_mask;
+    J.qmax = jp.qmax;
+    J.sign = jp.sign;
+    J.pad = 0;
+    pmax_all = std::max(pmax_all, jp.pmax);
+    qmax_all = std::max(qmax_all, std::min(jp.qmax, isqrt64(jp.pmax - 1)));
+  }
+  const uint32_t* dq = nullptr;
+  BaseTable bt;
+  if ((rc = prepare_sieving_primes(e, qmax_all, pmax_all, &dq, &bt))) return rc;
+  if (njobs) CU(cudaMemcpyAsync(b->jobs.p, hj.data(), njobs * sizeof(BJob), cudaMemcpyHostToDevice, e->st));
+  CU(cudaMemsetAsync(b->job_primes.p, 0, njobs * sizeof(unsigned long long), e->st));
+  CU(cudaMemsetAsync(b->job_sum.p, 0, njobs * sizeof(unsigned long long), e->st));
+  CU(cudaMemsetAsync(b->counters.p, 0, 4 * sizeof(uint32_t), e->st));
+
+  // batches, most expensive jobs first (steps per prime x range width)
+  std::vector<size_t> order(njobs);
+  for (size_t j = 0; j < njobs; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    const double cx = (double)hj[x].nsteps * (double)(jobs[x].pmax - jobs[x].pmin);
+    const double cy = (double)hj[y].nsteps * (double)(jobs[y].pmax - jobs[y].pmin);
+    return cx > cy;
+  });
+  std::vector<BBatch> all;
+  for (size_t oi = 0; oi < njobs; ++oi) {
+    const size_t j = order[oi];
+    const pps_job_params& jp = jobs[j];
+    const uint64_t lo0 = jp.pmin | 1ull;
+    if (jp.pmax <= lo0) continue;
+    const uint64_t span = 2ull * SEG_BITS * BATCH_SEGS;
+    for (uint64_t lo = lo0; lo < jp.pmax; lo += span) {
+      const uint64_t hi = std::min(jp.pmax, lo + span);
+      BBatch B;
+      memset(&B, 0, sizeof B);
+      B.lo = lo;
+      B.nbits = (hi - lo + 1) / 2;
+      B.job = (uint32_t)j;
+      B.limit = std::min(jp.qmax, isqrt64(hi - 1));
+      all.push_back(B);
+    }
+  }
+
+  // walk tile choice: chunk size and unroll, timed on a sample of the first wave
+  auto nseg_of = [](const BBatch& B) { return (uint32_t)((B.nbits + SEG_BITS - 1) / SEG_BITS); };
+  size_t next = 0;
+  int waves = 0;
+  bool tuned = b->tuned_chunk > 0;
+  while (next < all.size()) {
+    WaveTables* T = b->h_tables;
+    CU(cudaEventSynchronize(b->copied));  // staging free again
+    uint32_t nseg = 0, nb = 0;
+    while (next < all.size() && nb < WAVE_BATCHES) {
+      BBatch B = all[next];
+      const uint32_t ns = nseg_of(B);
+      if (nseg + ns > WAVE_SEGS) break;
+      B.seg0 = nseg;
+      for (uint32_t s = 0; s < ns; ++s) {
+        BSeg& S = T->seg[nseg + s];
+        S.lo = B.lo + 2ull * (uint64_t)s * SEG_BITS;
+        const uint64_t left = B.nbits - (uint64_t)s * SEG_BITS;
+        S.bits = (uint32_t)std::min<uint64_t>(left, SEG_BITS);
+        S.batch = nb;
+      }
+      T->batch[nb++] = B;
+      nseg += ns;
+      ++next;
+    }
+    T->nseg = nseg;
+    T->nbatch = nb;
+    const size_t bytes = offsetof(WaveTables, seg) + sizeof(BSeg) * WAVE_SEGS + sizeof(BBatch) * nb;
+    CU(cudaMemcpyAsync(b->tables.p, T, bytes, cudaMemcpyHostToDevice, e->st));
+    CU(cudaEventRecord(b->copied, e->st));
+
+    if (!tuned) {
+      // time each (chunk, unroll) on the first 2% of this wave's chunks
+      const int chunks[] = {32, 64, 128};
+      const int unrolls[] = {8, 16};
+      float best = 1e30f;
+      for (int c : chunks)
+        for (int u : unrolls) {
+          CU(cudaMemsetAsync(b->counters.p + 2, 0, sizeof(uint32_t), e->st));
+          // tuning hits go to the survivors' buffer tail, then are dropped
+          const uint64_t lim = std::max<uint64_t>(64, (uint64_t)nseg * 4);
+          if ((rc = launch_wave(e, dq, bt.nq, c, u, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n)))
+            return rc;
+          CU(cudaEventRecord(e->ev[0], e->st));
+          CU(cudaMemsetAsync(b->tot.p + 3, 0, sizeof(uint64_t), e->st));
+          auto fn = u == 16 ? k_bwalk<16> : k_bwalk<8>;
+          int per_sm = 0;
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
+          fn<<<std::max(per_sm, 1) * e->num_sms, BW_THREADS, 0, e->st>>>(
+              b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->P.p, b->Pinv.p, b->tot.p,
+              (uint32_t)c, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
+          CU(cudaEventRecord(e->ev[1], e->st));
+          CU(cudaEventSynchronize(e->ev[1]));
+          float ms = 0;
+          CU(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
+          if (ms < best) {
+            best = ms;
+            b->tuned_chunk = c;
+            b->tuned_unroll = u;
+          }
+        }
+      // the tuning waves added to the per-job prime counts: clear them
+      CU(cudaMemsetAsync(b->job_primes.p, 0, njobs * sizeof(unsigned long long), e->st));
+      CU(cudaMemsetAsync(b->job_sum.p, 0, njobs * sizeof(unsigned long long), e->st));
+      e->launches += 6;
+      tuned = true;
+    }
+    // the wave itself: a captured graph of the fixed sequence, replayed
+    if (!b->graph || b->graph_chunk != b->tuned_chunk || b->graph_unroll != b->tuned_unroll) {
+      if (b->graph) cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+      cudaGraph_t g;
+      CU(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+      const uint64_t launches0 = e->launches;
+      rc = launch_wave(e, dq, bt.nq, b->tuned_chunk, b->tuned_unroll, 0, b->hits.p, b->counters.p,
+                       (uint32_t)b->hits.n);
+      cudaError_t ce = cudaStreamEndCapture(e->st, &g);
+      e->launches = launches0;
+      if (rc) return rc;
+      if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+      b->graph_chunk = b->tuned_chunk;
+      b->graph_unroll = b->tuned_unroll;
+    }
+    CU(cudaGraphLaunch(b->graph, e->st));
+    e->launches += 9;
+    ++waves;
+  }
+
+  // output rule, then group by job
+  CU(cudaEventRecord(e->ev[4], e->st));
+  CU(cudaMemcpyAsync(e->h_pinned, b->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
+  CU(cudaStreamSynchronize(e->st));
+  const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
+  if (raw > b->hits.n) {
+    // more candidates than the buffer: grow it and run the whole batch again
+    if ((rc = b->hits.ensure((size_t)raw * 2))) return rc;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    return pps_run_batch(e, jobs, njobs, out, cap, nout, job_offsets, bst);
+  }
+  if (raw) {
+    uint32_t blocks = (raw * 32u + 255u) / 256u;
+    if (blocks > 4096u) blocks = 4096u;
+    k_bfilter<<<blocks, 256, 0, e->st>>>(b->hits.p, b->counters.p, (uint32_t)b->hits.n, b->jobs.p, e->small_q.p,
+                                         e->nsmall, b->out.p, b->counters.p + 1, (uint32_t)b->out.n);
+    CU(cudaGetLastError());
+    e->launches++;
+  }
+  CU(cudaEventRecord(e->ev[5], e->st));
+  CU(cudaMemcpyAsync(e->h_pinned, b->counters.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
+  CU(cudaStreamSynchronize(e->st));
+  const uint32_t nf = ((uint32_t*)e->h_pinned)[1];
+  if (nf > b->out.n) return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "%u factors exceed the batch buffer", nf);
+  std::vector<pps_hit> surv(nf);
+  if (nf) CU(cudaMemcpy(surv.data(), b->out.p, nf * sizeof(pps_hit), cudaMemcpyDeviceToHost));
+  std::sort(surv.begin(), surv.end(), [](const pps_hit& x, const pps_hit& y) {
+    if (x.idx != y.idx) return x.idx < y.idx;
+    if (x.p != y.p) return x.p < y.p;
+    if (x.k != y.k) return x.k < y.k;
+    return x.n < y.n;
+  });
+  if (nout) *nout = nf;
+  if (job_offsets) {
+    size_t k = 0;
+    for (size_t j = 0; j <= njobs; ++j) {
+      while (k < nf && surv[k].idx < j) ++k;
+      job_offsets[j] = k;
+    }
+  }
+  if (out) {
+    for (size_t i = 0; i < nf && i < cap; ++i) {
+      out[i].p = surv[i].p;
+      out[i].k = surv[i].k;
+      out[i].n = surv[i].n;
+      out[i].c = jobs[surv[i].idx].sign;
+    }
+  }
+  if (bst) {
+    std::vector<unsigned long long> jp(njobs), js(njobs);
+    if (njobs) {
+      CU(cudaMemcpy(jp.data(), b->job_primes.p, njobs * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+      CU(cudaMemcpy(js.data(), b->job_sum.p, njobs * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    }
+    for (size_t j = 0; j < njobs; ++j) {
+      bst->primes += jp[j];
+      bst->prime_sum += js[j];
+      bst->steps += jp[j] * hj[j].nsteps;
+    }
+    bst->raw_hits = raw;
+    bst->factors = nf;
+    bst->waves = (uint32_t)waves;
+    bst->chunk = (uint32_t)b->tuned_chunk;
+    bst->unroll = (uint32_t)b->tuned_unroll;
+    float ms = 0, fms = 0;
+    CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[5]));
+    CU(cudaEventElapsedTime(&fms, e->ev[4], e->ev[5]));
+    bst->total_ms = ms;
+    bst->filter_ms = fms;
+  }
+  if (out && nf > cap) return set_err(PPS_ERR_OVERFLOW, "%u factors, buffer holds %zu", nf, cap);
+  return PPS_OK;
+}
+
+extern "C" int pps_batch_job_primes(pps_engine* e, size_t njobs, uint64_t* primes, uint64_t* sums) {
+  if (!e || !e->batch || !e->batch->ready) return set_err(PPS_ERR_INVALID_PARAM, "no batch has run");
+  if (njobs > e->batch->job_primes.n) return set_err(PPS_ERR_INVALID_PARAM, "njobs too large");
+  CU(cudaSetDevice(e->device));
+  if (primes) CU(cudaMemcpy(primes, e->batch->job_primes.p, njobs * 8, cudaMemcpyDeviceToHost));
+  if (sums) CU(cudaMemcpy(sums, e->batch->job_sum.p, njobs * 8, cudaMemcpyDeviceToHost));
+  return PPS_OK;
+}

@@ -20,6 +20,7 @@
 #include <mutex>
 #include <vector>
 
+#include "pps_engine_impl.h"
 #include "pps_internal.h"
 #include "ppsgpu.h"
 
@@ -28,7 +29,7 @@ using namespace pps;
 // --------------------------------------------------------------- errors
 static thread_local char g_err[512];
 
-static int set_err(int code, const char* fmt, ...) {
+int set_err(int code, const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
   vsnprintf(g_err, sizeof g_err, fmt, ap);
@@ -38,14 +39,6 @@ static int set_err(int code, const char* fmt, ...) {
 
 extern "C" const char* pps_last_error(void) { return g_err; }
 extern "C" const char* pps_version(void) { return "ppsgpu-0.1 (sm_103a)"; }
-
-#define CU(call)                                                                         \
-  do {                                                                                   \
-    cudaError_t e_ = (call);                                                             \
-    if (e_ != cudaSuccess)                                                               \
-      return set_err(PPS_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),      \
-                     __FILE__, __LINE__);                                                \
-  } while (0)
 
 // ------------------------------------------------------------ normalize
 static int lg2u64(uint64_t v) {
@@ -115,62 +108,6 @@ extern "C" int pps_normalize(const pps_job_spec* in, pps_job_params* o) {
 }
 
 // ---------------------------------------------------------------- engine
-template <typename T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  int ensure(size_t want) {
-    if (want <= n) return PPS_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-    size_t grow = want + want / 8;
-    cudaError_t e = cudaMalloc(&p, grow * sizeof(T));
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      p = nullptr;
-      return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "cudaMalloc(%zu bytes): %s",
-                     grow * sizeof(T), cudaGetErrorString(e));
-    }
-    n = grow;
-    return PPS_OK;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  size_t bytes() const { return n * sizeof(T); }
-};
-
-struct pps_engine {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t st = nullptr;
-  cudaEvent_t ev[8] = {};
-  uint64_t batch_span = 1ull << 31;
-  int forced_variant = -1;
-  int tuned_variant[2] = {-1, -1};  // [step==32]
-  uint64_t launches = 0;
-
-  // sieving primes (ascending odd primes <= base_limit), u32
-  DevBuf<uint32_t> base_q;
-  uint32_t base_limit = 0;
-  uint32_t base_count = 0;
-  std::vector<uint32_t> host_seed;  // odd primes < SEG_BITS (host copy)
-  DevBuf<uint32_t> seed_q;
-
-  DevBuf<uint32_t> bitmap, seg_count, seg_off;
-  DevBuf<uint64_t> P, Pinv;
-  DevBuf<uint64_t> totals;  // [0] count, [1] sum
-  DevBuf<pps_hit> hits;
-  DevBuf<pps_factor> factors;
-  DevBuf<uint32_t> counters;  // [0] raw hits, [1] factors
-  DevBuf<uint16_t> small_q;
-  uint32_t nsmall = 0;
-  DevBuf<uint32_t> probe_sink;
-  uint64_t* h_pinned = nullptr;  // 16 words of pinned host scratch
-};
 
 static void free_engine(pps_engine* e) {
   if (!e) return;
@@ -188,6 +125,7 @@ static void free_engine(pps_engine* e) {
   e->counters.release();
   e->small_q.release();
   e->probe_sink.release();
+  batch_state_free(e);
   if (e->h_pinned) cudaFreeHost(e->h_pinned);
   for (auto& v : e->ev)
     if (v) cudaEventDestroy(v);
@@ -275,7 +213,7 @@ extern "C" int pps_engine_set_variant(pps_engine* e, int v) {
 extern "C" uint64_t pps_engine_launches(const pps_engine* e) { return e ? e->launches : 0; }
 
 // ----------------------------------------------------------------- sieve
-static uint32_t isqrt64(uint64_t x) {
+uint32_t isqrt64(uint64_t x) {
   uint64_t r = (uint64_t)sqrt((double)x);
   while (r * r > x) r--;
   while ((r + 1) * (r + 1) <= x) r++;
@@ -312,9 +250,6 @@ static uint32_t count_le(const std::vector<uint32_t>& v, uint32_t x) {
   return (uint32_t)(std::upper_bound(v.begin(), v.end(), x) - v.begin());
 }
 
-struct BaseTable {
-  uint32_t nq, nq_tiny, nq_seg;
-};
 
 // Make sure the device holds all odd primes <= limit and fill the counts.
 // Returns 1 when the host-made seed table (odd primes < SEG_BITS) serves,
@@ -372,7 +307,7 @@ static int ensure_base(pps_engine* e, uint32_t limit, BaseTable* bt) {
   return 0;
 }
 
-static int prepare_sieving_primes(pps_engine* e, uint32_t qmax, uint64_t pmax, const uint32_t** dq,
+int prepare_sieving_primes(pps_engine* e, uint32_t qmax, uint64_t pmax, const uint32_t** dq,
                                   BaseTable* bt) {
   // only q with q*q < pmax can matter
   uint32_t lim = qmax;

@@ -1,0 +1,93 @@
+// pps_engine_impl.h -- engine state shared by the library's host translation
+// units (pps_engine.cu, pps_batch.cu, pps_server.cu).  Not part of the ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "pps_internal.h"
+#include "ppsgpu.h"
+
+// Record an error for pps_last_error(); returns code.
+int set_err(int code, const char* fmt, ...);
+
+#define CU(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return set_err(PPS_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),      \
+                     __FILE__, __LINE__);                                                \
+  } while (0)
+
+// Device buffer that only grows (contents are not preserved on growth).
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  int ensure(size_t want) {
+    if (want <= n) return PPS_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    size_t grow = want + want / 8;
+    cudaError_t e = cudaMalloc(&p, grow * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "cudaMalloc(%zu bytes): %s",
+                     grow * sizeof(T), cudaGetErrorString(e));
+    }
+    n = grow;
+    return PPS_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+struct BatchState;  // pps_batch.cu
+
+struct pps_engine {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[8] = {};
+  uint64_t batch_span = 1ull << 31;
+  int forced_variant = -1;
+  int tuned_variant[2] = {-1, -1};  // [step==32]
+  uint64_t launches = 0;
+
+  // sieving primes (ascending odd primes <= base_limit), u32
+  DevBuf<uint32_t> base_q;
+  uint32_t base_limit = 0;
+  uint32_t base_count = 0;
+  std::vector<uint32_t> host_seed;  // odd primes < SEG_BITS (host copy)
+  DevBuf<uint32_t> seed_q;
+
+  DevBuf<uint32_t> bitmap, seg_count, seg_off;
+  DevBuf<uint64_t> P, Pinv;
+  DevBuf<uint64_t> totals;  // [0] count, [1] sum
+  DevBuf<pps_hit> hits;
+  DevBuf<pps_factor> factors;
+  DevBuf<uint32_t> counters;  // [0] raw hits, [1] factors
+  DevBuf<uint16_t> small_q;
+  uint32_t nsmall = 0;
+  DevBuf<uint32_t> probe_sink;
+  uint64_t* h_pinned = nullptr;  // 16 words of pinned host scratch
+
+  BatchState* batch = nullptr;  // state of the batched persistent form
+};
+
+struct BaseTable {
+  uint32_t nq, nq_tiny, nq_seg;
+};
+
+uint32_t isqrt64(uint64_t x);
+// Device table of odd sieving primes q <= min(qmax, sqrt(pmax-1)), with counts.
+int prepare_sieving_primes(pps_engine* e, uint32_t qmax, uint64_t pmax, const uint32_t** dq,
+                           BaseTable* bt);
+void batch_state_free(pps_engine* e);

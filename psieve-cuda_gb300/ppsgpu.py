@@ -69,6 +69,18 @@ class JobStats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class BatchStats(ctypes.Structure):
+    _fields_ = [("primes", ctypes.c_uint64), ("prime_sum", ctypes.c_uint64),
+                ("raw_hits", ctypes.c_uint64), ("factors", ctypes.c_uint64),
+                ("steps", ctypes.c_uint64), ("waves", ctypes.c_uint32),
+                ("chunk", ctypes.c_uint32), ("unroll", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32), ("total_ms", ctypes.c_double),
+                ("filter_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
 class PPSError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"ppsgpu error {code}: {msg}")
@@ -115,6 +127,10 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_check_primes_noalloc": (ctypes.c_int, [P(JobParams), ctypes.c_void_p, ctypes.c_size_t,
                                                     ctypes.c_void_p, ctypes.c_uint32,
                                                     P(ctypes.c_uint32), ctypes.c_void_p]),
+        "pps_run_batch": (ctypes.c_int, [ctypes.c_void_p, P(JobParams), ctypes.c_size_t,
+                                         ctypes.c_void_p, ctypes.c_size_t, szp, szp,
+                                         P(BatchStats)]),
+        "pps_batch_job_primes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, u64p, u64p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -247,3 +263,81 @@ class Engine:
         v = ctypes.c_double()
         _check(self.lib, self.lib.pps_measure_imad_peak(self.h, ctypes.byref(v)))
         return v.value
+
+    def run_batch(self, jobs: list, cap: int = 1 << 18):
+        """Batched persistent form: returns (list of per-job factor arrays, BatchStats)."""
+        arr = (JobParams * max(len(jobs), 1))(*jobs)
+        offs = (ctypes.c_size_t * (len(jobs) + 1))()
+        while True:
+            out = np.zeros(cap, dtype=FACTOR_DTYPE)
+            n = ctypes.c_size_t()
+            st = BatchStats()
+            rc = self.lib.pps_run_batch(self.h, arr, len(jobs), out.ctypes.data_as(ctypes.c_void_p),
+                                        cap, ctypes.byref(n), offs, ctypes.byref(st))
+            if rc == PPS_ERR_OVERFLOW and n.value > cap:
+                cap = n.value
+                continue
+            _check(self.lib, rc)
+            per = [out[offs[j]:offs[j + 1]].copy() for j in range(len(jobs))]
+            return per, st
+
+    def batch_job_primes(self, njobs: int):
+        pr = np.zeros(max(njobs, 1), dtype=np.uint64)
+        sm = np.zeros(max(njobs, 1), dtype=np.uint64)
+        _check(self.lib, self.lib.pps_batch_job_primes(
+            self.h, njobs, pr.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+            sm.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+        return pr[:njobs], sm[:njobs]
+
+
+def normalize_or_repair(spec: dict, lib=None):
+    """Normalise like the reference; where the reference would refuse a job,
+    repair it the way its own message suggests and record the repair:
+      pmin <= 2^32              -> pmin = 2^32 + 1 (pps/appcu.cu:236-239)
+      2^(64-nstep) > pmin       -> double pmin until the rule holds
+                                   (the "will work by the time pmin ==" loop,
+                                   pps/appcu.cu:163-176)
+    The p width is kept.  Returns (JobParams, list of repair strings)."""
+    spec = dict(spec)
+    repairs = []
+    width = spec["pmax"] - spec["pmin"]
+    for _ in range(80):
+        try:
+            return normalize(**spec, lib=lib), repairs
+        except PPSError as e:
+            msg = str(e)
+            if "<= 2^32" in msg:
+                spec["pmin"] = (1 << 32) + 1
+            elif "pmin is not large enough" in msg:
+                spec["pmin"] *= 2
+            else:
+                raise
+            spec["pmax"] = spec["pmin"] + width
+            repairs.append(f"pmin->{spec['pmin']}")
+    raise PPSError(PPS_ERR_INVALID_PARAM, f"could not repair {spec}")
+
+
+def mixed_jobs(seed: int = 1, count: int = 512, scale_p: float = 1.0, scale_n: float = 1.0,
+               lib=None):
+    """The mixed-job workload: `count` jobs drawn from `seed`.  Side +/- uniform;
+    kmin odd uniform in [3, 5000]; k width log-uniform in [1e2, 1e4]; nmin uniform
+    in [1e3, 1e6]; n width log-uniform in [1e2, 1e6]; pmin log-uniform in
+    [1e10, 2^61]; p width log-uniform in [1e7, 1e9] (p > kmax always holds).
+    scale_p / scale_n shrink the p and n widths for quick tests.  Returns
+    (list of JobParams, list of (spec, repairs))."""
+    rng = np.random.default_rng(seed)
+    jobs, meta = [], []
+    for _ in range(count):
+        sign = 1 if rng.integers(0, 2) else -1
+        kmin = int(rng.integers(1, 2500)) * 2 + 1
+        kw = int(10 ** rng.uniform(2, 4))
+        nmin = int(rng.integers(1000, 1000001))
+        nw = max(50, int(10 ** rng.uniform(2, 6) * scale_n))
+        pmin = int(10 ** rng.uniform(10, np.log10(2.0 ** 61)))
+        pw = max(1000, int(10 ** rng.uniform(7, 9) * scale_p))
+        spec = dict(pmin=pmin, pmax=pmin + pw, kmin=kmin, kmax=kmin + kw, nmin=nmin, nmax=nmin + nw,
+                    sign=sign)
+        jp, repairs = normalize_or_repair(spec, lib=lib)
+        jobs.append(jp)
+        meta.append((spec, repairs))
+    return jobs, meta

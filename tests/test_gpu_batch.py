@@ -1,0 +1,56 @@
+"""The batched persistent form (pps_run_batch) on the GPU: every job's factor
+list and prime fingerprint must be exactly what the one-job path and the
+reference give for that job alone."""
+from __future__ import annotations
+
+import pytest
+
+from helpers import args_to_spec, lines_of
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_reference_random_jobs(pps, engine, ref_cases):
+    names = sorted(k for k in ref_cases if k.startswith("rand"))
+    jobs = [pps.normalize(**args_to_spec(ref_cases[n]["args"])) for n in names]
+    per, st = engine.run_batch(jobs)
+    pr, _ = engine.batch_job_primes(len(jobs))
+    for j, name in enumerate(names):
+        case = ref_cases[name]
+        assert lines_of(pps.factors_to_tuples(per[j])) == sorted(set(case["lines"])), name
+        assert int(pr[j]) == case["count"], name
+    assert st.primes == sum(ref_cases[n]["count"] for n in names)
+
+
+def test_batch_equals_single_jobs_mixed(pps, engine):
+    jobs, meta = pps.mixed_jobs(seed=7, count=48, scale_p=2e-3, scale_n=2e-2)
+    per, st = engine.run_batch(jobs)
+    pr, sm = engine.batch_job_primes(len(jobs))
+    total = 0
+    for j, jp in enumerate(jobs):
+        want, wst = engine.run_job(jp)
+        assert pps.factors_to_tuples(per[j]) == pps.factors_to_tuples(want), (j, meta[j])
+        assert int(pr[j]) == wst.primes and int(sm[j]) == wst.prime_sum, (j, meta[j])
+        total += len(want)
+    assert st.factors == total
+    assert st.waves >= 1 and st.chunk in (32, 64, 128) and st.unroll in (8, 16)
+
+
+def test_batch_repeat_and_degenerate(pps, engine, ora):
+    base = [
+        dict(pmin=10**12, pmax=10**12 + 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=6000),
+        dict(pmin=10**12 + 40, pmax=10**12 + 60, kmin=1201, kmax=9999, nmin=2000, nmax=3000),  # no primes
+        dict(pmin=(1 << 62) - 10**6, pmax=1 << 62, kmin=3, kmax=9999, nmin=1000, nmax=1002, sign=-1),
+        dict(pmin=42 * 10**12, pmax=42 * 10**12 + 10**6, kmin=1201, kmax=9999, nmin=2000000,
+             nmax=2100000),
+    ]
+    jobs = [pps.normalize(**s) for s in base]
+    first, _ = engine.run_batch(jobs)
+    second, _ = engine.run_batch(jobs)  # graph replay path
+    for j, spec in enumerate(base):
+        want, _, _ = ora.run(ora.normalize(**spec))
+        assert pps.factors_to_tuples(first[j]) == ora.tuples(want), spec
+        assert pps.factors_to_tuples(second[j]) == ora.tuples(want), spec
+    # an empty batch is valid
+    per, st = engine.run_batch([])
+    assert per == [] and st.factors == 0
