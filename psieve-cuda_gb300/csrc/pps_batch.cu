@@ -79,6 +79,8 @@ struct BatchState {
   uint64_t prime_cap = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_chunk = 0, graph_unroll = 0;
+  const uint32_t* graph_q = nullptr;  // sieving-prime table the graph was captured with
+  uint32_t graph_nq = 0;
   cudaEvent_t copied = nullptr;
   int tuned_chunk = 0, tuned_unroll = 0;
 };
@@ -542,10 +544,13 @@ int ensure_state(pps_engine* e, size_t njobs) {
     if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
     if (cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming) != cudaSuccess)
       return set_err(PPS_ERR_CUDA, "event");
+    // job tables at their maximum size once: the captured graph holds these pointers
+    if ((rc = b->jobs.ensure(MAX_JOBS)) || (rc = b->job_primes.ensure(MAX_JOBS)) ||
+        (rc = b->job_sum.ensure(MAX_JOBS)))
+      return rc;
     b->ready = true;
   }
-  if ((rc = b->jobs.ensure(njobs)) || (rc = b->job_primes.ensure(njobs)) || (rc = b->job_sum.ensure(njobs)))
-    return rc;
+  (void)njobs;
   return PPS_OK;
 }
 
@@ -720,7 +725,8 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
       tuned = true;
     }
     // the wave itself: a captured graph of the fixed sequence, replayed
-    if (!b->graph || b->graph_chunk != b->tuned_chunk || b->graph_unroll != b->tuned_unroll) {
+    if (!b->graph || b->graph_chunk != b->tuned_chunk || b->graph_unroll != b->tuned_unroll ||
+        b->graph_q != dq || b->graph_nq != bt.nq) {
       if (b->graph) cudaGraphExecDestroy(b->graph);
       b->graph = nullptr;
       cudaGraph_t g;
@@ -737,6 +743,8 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
       if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
       b->graph_chunk = b->tuned_chunk;
       b->graph_unroll = b->tuned_unroll;
+      b->graph_q = dq;
+      b->graph_nq = bt.nq;
     }
     CU(cudaGraphLaunch(b->graph, e->st));
     e->launches += 9;
