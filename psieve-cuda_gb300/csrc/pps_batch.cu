@@ -70,7 +70,7 @@ struct BatchState {
   WaveTables* h_tables = nullptr;
   DevBuf<BJob> jobs;
   DevBuf<uint32_t> bitmap;      // WAVE_SEGS * SEG_WORDS
-  DevBuf<uint32_t> seg_count, seg_off, chunk_count, chunk_off;
+  DevBuf<uint32_t> seg_count, seg_off, chunk_count, chunk_off, chunk_seg;
   DevBuf<uint64_t> P, Pinv;
   DevBuf<uint64_t> tot;         // [0] primes, [1] sum, [2] chunks, [3] work counter
   DevBuf<unsigned long long> job_primes, job_sum;
@@ -98,6 +98,7 @@ void batch_state_free(pps_engine* e) {
   b->seg_off.release();
   b->chunk_count.release();
   b->chunk_off.release();
+  b->chunk_seg.release();
   b->P.release();
   b->Pinv.release();
   b->tot.release();
@@ -319,6 +320,17 @@ __global__ void k_bchunks(const uint8_t* tables, const uint32_t* seg_count, uint
     chunk_count[s] = s < T->nseg ? (seg_count[s] + chunk - 1) / chunk : 0u;
 }
 
+// chunk -> segment map (one CTA per segment writes its chunks' entries)
+__global__ void k_bchunkmap(const uint8_t* tables, const uint32_t* chunk_count, const uint32_t* chunk_off,
+                            uint32_t* chunk_seg, uint64_t map_cap) {
+  const WaveTables* T = wt(tables);
+  const uint32_t s = blockIdx.x;
+  if (s >= T->nseg) return;
+  const uint32_t c0 = chunk_off[s], n = chunk_count[s];
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    if ((uint64_t)c0 + i < map_cap) chunk_seg[c0 + i] = s;
+}
+
 __device__ __forceinline__ void b_record(uint32_t klo, uint32_t khi, uint32_t n, uint32_t step, uint64_t p,
                                          uint32_t job, const BJob& J, pps_hit* hits, uint32_t* hit_count,
                                          uint32_t hit_cap) {
@@ -359,7 +371,7 @@ __device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t pl
 // exactly once the round's walks are done.
 template <bool S32, int U>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
-                                        uint32_t* qe, uint32_t* qc, uint64_t* qp, pps_hit* hits,
+                                        uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
                                         uint32_t* hit_count, uint32_t hit_cap) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t s = S32 ? 32u : J.step;
@@ -385,6 +397,8 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
       }
     }
     if (full * (uint32_t)U < nsteps) {
+      // the partial last block: its start value is at hand, keep it
+      qk[lane] = mk64(klo, khi);
       const uint32_t pos = atomicAdd(qc, 1u);
       if (pos < BQ_CAP) qe[pos] = (lane << 27) | full;
     }
@@ -400,8 +414,13 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
       const uint32_t t0 = (uint32_t)U * blk;
       const uint32_t nblk = min((uint32_t)U, nsteps - t0);
       const uint32_t n0 = J.nmin + s * t0;
-      const uint64_t x = inv_pow2(n0, op, ops);
-      const uint64_t K = J.proth ? op - x : x;
+      uint64_t K;
+      if (blk == full) {
+        K = qk[owner];
+      } else {
+        const uint64_t x = inv_pow2(n0, op, ops);
+        K = J.proth ? op - x : x;
+      }
       uint32_t klo = lo32(K), khi = hi32(K);
       const uint32_t oplo = lo32(op), ophi = hi32(op);
       const uint32_t opinv = S32 ? lo32(ops) : (lo32(ops) << (32u - s));
@@ -431,15 +450,15 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
 template <int U>
 __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, const BJob* jobs,
                                                          const uint32_t* seg_count, const uint32_t* seg_off,
-                                                         const uint32_t* chunk_off, const uint64_t* P,
-                                                         const uint64_t* Pinv, uint64_t* tot, uint32_t chunk,
-                                                         uint64_t chunk_limit, pps_hit* hits,
+                                                         const uint32_t* chunk_off, const uint32_t* chunk_seg,
+                                                         const uint64_t* P, const uint64_t* Pinv, uint64_t* tot,
+                                                         uint32_t chunk, uint64_t chunk_limit, pps_hit* hits,
                                                          uint32_t* hit_count, uint32_t hit_cap) {
   __shared__ uint32_t q_ent[BW_THREADS / 32][BQ_CAP];
   __shared__ uint64_t q_p[BW_THREADS / 32][32];
+  __shared__ uint64_t q_k[BW_THREADS / 32][32];
   __shared__ uint32_t q_cnt[BW_THREADS / 32];
   const WaveTables* T = wt(tables);
-  const uint32_t nseg = T->nseg;
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   uint64_t nchunks = tot[2];
   if (chunk_limit && chunk_limit < nchunks) nchunks = chunk_limit;
@@ -450,13 +469,7 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
     if (lane == 0) c = atomicAdd((unsigned long long*)&tot[3], 1ull);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= nchunks) break;
-    // segment of chunk c: last s with chunk_off[s] <= c
-    uint32_t lo = 0, hi = nseg;
-    while (lo < hi) {
-      const uint32_t mid = lo + (hi - lo) / 2;
-      if ((uint64_t)chunk_off[mid] <= c) lo = mid + 1; else hi = mid;
-    }
-    const uint32_t s = lo - 1;
+    const uint32_t s = chunk_seg[c];
     const uint32_t job = T->batch[T->seg[s].batch].job;
     const BJob J = jobs[job];
     const uint32_t within = (uint32_t)(c - chunk_off[s]) * chunk;
@@ -467,9 +480,11 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
       const uint64_t pi = first + r + (valid ? lane : 0u);
       const uint64_t p = P[pi], ps = Pinv[pi];
       if (J.step == 32)
-        b_round<true, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], hits, hit_count, hit_cap);
+        b_round<true, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, hit_count,
+                         hit_cap);
       else
-        b_round<false, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], hits, hit_count, hit_cap);
+        b_round<false, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, hit_count,
+                          hit_cap);
     }
   }
 }
@@ -539,6 +554,8 @@ int ensure_state(pps_engine* e, size_t njobs) {
     // p > 2^32: odd primes are fewer than 1/10 of the odd candidates
     b->prime_cap = (uint64_t)WAVE_SEGS * SEG_BITS / 10 + 4096;
     if ((rc = b->P.ensure(b->prime_cap)) || (rc = b->Pinv.ensure(b->prime_cap))) return rc;
+    // at most prime_cap/32 + one partial chunk per segment (smallest chunk: 32)
+    if ((rc = b->chunk_seg.ensure(b->prime_cap / 32 + WAVE_SEGS))) return rc;
     if ((rc = b->tot.ensure(4))) return rc;
     if ((rc = b->counters.ensure(4))) return rc;
     if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
@@ -569,14 +586,17 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int chunk, i
                                                   b->job_primes.p, b->job_sum.p, b->prime_cap);
   k_bchunks<<<(WAVE_SEGS + 255) / 256, 256, 0, st>>>(b->tables.p, b->seg_count.p, b->chunk_count.p, chunk);
   k_bscan<<<1, 1024, 0, st>>>(b->chunk_count.p, b->chunk_off.p, WAVE_SEGS, b->tot.p + 2);
+  k_bchunkmap<<<WAVE_SEGS, 256, 0, st>>>(b->tables.p, b->chunk_count.p, b->chunk_off.p, b->chunk_seg.p,
+                                         b->chunk_seg.n);
   int per_sm = 0;
   auto fn = unroll == 16 ? k_bwalk<16> : k_bwalk<8>;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
   const int grid = (per_sm > 0 ? per_sm : 1) * e->num_sms;
-  fn<<<grid, BW_THREADS, 0, st>>>(b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->P.p,
-                                  b->Pinv.p, b->tot.p, (uint32_t)chunk, chunk_limit, hits, hit_count, hit_cap);
+  fn<<<grid, BW_THREADS, 0, st>>>(b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p,
+                                  b->chunk_seg.p, b->P.p, b->Pinv.p, b->tot.p, (uint32_t)chunk, chunk_limit, hits,
+                                  hit_count, hit_cap);
   CU(cudaGetLastError());
-  e->launches += 9;
+  e->launches += 10;
   return PPS_OK;
 }
 
@@ -706,8 +726,8 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
           int per_sm = 0;
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
           fn<<<std::max(per_sm, 1) * e->num_sms, BW_THREADS, 0, e->st>>>(
-              b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->P.p, b->Pinv.p, b->tot.p,
-              (uint32_t)c, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
+              b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->chunk_seg.p, b->P.p,
+              b->Pinv.p, b->tot.p, (uint32_t)c, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
           CU(cudaEventRecord(e->ev[1], e->st));
           CU(cudaEventSynchronize(e->ev[1]));
           float ms = 0;

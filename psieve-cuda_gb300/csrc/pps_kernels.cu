@@ -395,6 +395,7 @@ template <int TEST, int U, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
   __shared__ uint32_t q_ent[WQ_WARPS][WQ_CAP];
   __shared__ uint64_t q_p[WQ_WARPS][32];
+  __shared__ uint64_t q_k[WQ_WARPS][32];  // start value of each lane's partial last block
   __shared__ uint32_t q_cnt[WQ_WARPS];
   const uint64_t np = a.d_np ? *a.d_np : a.np;
   const uint32_t win_hi = a.win_hi, win_mask = a.win_mask, bound_hi = a.bound_hi;
@@ -432,8 +433,10 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
           if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | b;
         }
       }
-      // the last partial block (fewer than U steps) always goes to the queue
+      // the last partial block (fewer than U steps) always goes to the queue,
+      // with its start value, which is at hand
       if (full * (uint32_t)U < nsteps) {
+        q_k[wib][lane] = mk64(klo, khi);
         const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
         if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | full;
       }
@@ -450,8 +453,13 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         const uint32_t t0 = (uint32_t)U * blk;
         const uint32_t nblk = min((uint32_t)U, nsteps - t0);
         const uint32_t n0 = nmin + 32u * t0;
-        const uint64_t x = inv_pow2(n0, op, ops);
-        const uint64_t K = a.proth ? op - x : x;
+        uint64_t K;
+        if (blk == full) {
+          K = q_k[wib][owner];
+        } else {
+          const uint64_t x = inv_pow2(n0, op, ops);
+          K = a.proth ? op - x : x;
+        }
         uint32_t klo = lo32(K), khi = hi32(K);
         const uint32_t oplo = lo32(op), ophi = hi32(op), opinv = lo32(ops);
 #pragma unroll 1
