@@ -170,9 +170,11 @@ uint64_t pps_engine_launches(const pps_engine *e);
    different k, n and p ranges, mixed signs -- are sieved wave by wave into one
    device prime table and walked by one persistent kernel whose warps take
    chunks of primes from a device work counter; each wave's launch sequence is
-   a captured CUDA graph; the chunk size and unroll are tuned on the first
-   wave.  Factors come back grouped by job (job_offsets[j]..job_offsets[j+1]),
-   each group sorted by (p, k, n), exactly as pps_run_job would return them. */
+   a captured CUDA graph; the work per chunk (walk steps per lane: a job's
+   chunk holds work*32/nsteps primes) and the unroll are tuned on the first
+   wave and reported in `chunk` and `unroll`.  Factors come back grouped by
+   job (job_offsets[j]..job_offsets[j+1]), each group sorted by (p, k, n),
+   exactly as pps_run_job would return them. */
 typedef struct {
   uint64_t primes, prime_sum, raw_hits, factors, steps;
   uint32_t waves, chunk, unroll, pad;

@@ -34,13 +34,14 @@ constexpr uint32_t WAVE_BATCHES = WAVE_SEGS;    // at most one batch per segment
 constexpr uint32_t MAX_JOBS = 1u << 16;
 constexpr int BW_THREADS = 256;
 constexpr uint32_t BQ_CAP = 256;  // queued blocks per warp
+constexpr uint32_t MAX_CHUNK = 8192;  // primes per work chunk, at most (a multiple of 32)
 
 struct BJob {
   uint64_t kmin, kmax, kstep, koffset;
   uint32_t nmin, nmax, step, nsteps;
   uint32_t proth, win_hi, win_mask, qmax;
   int32_t sign;
-  uint32_t pad;
+  uint32_t chunk;  // primes per work chunk: about the same walk steps for every job
 };
 
 struct BBatch {
@@ -78,11 +79,11 @@ struct BatchState {
   DevBuf<uint32_t> counters;    // [0] raw, [1] survivors
   uint64_t prime_cap = 0;
   cudaGraphExec_t graph = nullptr;
-  int graph_chunk = 0, graph_unroll = 0;
+  int graph_unroll = 0;
   const uint32_t* graph_q = nullptr;  // sieving-prime table the graph was captured with
   uint32_t graph_nq = 0;
   cudaEvent_t copied = nullptr;
-  int tuned_chunk = 0, tuned_unroll = 0;
+  int tuned_work = 0, tuned_unroll = 0;  // walk steps per chunk (x32 lanes), inner unroll
 };
 
 void batch_state_free(pps_engine* e) {
@@ -313,11 +314,17 @@ __global__ void __launch_bounds__(SIEVE_THREADS) k_bexpand(const uint8_t* tables
   }
 }
 
-__global__ void k_bchunks(const uint8_t* tables, const uint32_t* seg_count, uint32_t* chunk_count,
-                          uint32_t chunk) {
+__global__ void k_bchunks(const uint8_t* tables, const BJob* jobs, const uint32_t* seg_count,
+                          uint32_t* chunk_count) {
   const WaveTables* T = wt(tables);
-  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < WAVE_SEGS; s += gridDim.x * blockDim.x)
-    chunk_count[s] = s < T->nseg ? (seg_count[s] + chunk - 1) / chunk : 0u;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < WAVE_SEGS; s += gridDim.x * blockDim.x) {
+    uint32_t n = 0;
+    if (s < T->nseg) {
+      const uint32_t chunk = jobs[T->batch[T->seg[s].batch].job].chunk;
+      n = (seg_count[s] + chunk - 1) / chunk;
+    }
+    chunk_count[s] = n;
+  }
 }
 
 // chunk -> segment map (one CTA per segment writes its chunks' entries)
@@ -452,7 +459,7 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
                                                          const uint32_t* seg_count, const uint32_t* seg_off,
                                                          const uint32_t* chunk_off, const uint32_t* chunk_seg,
                                                          const uint64_t* P, const uint64_t* Pinv, uint64_t* tot,
-                                                         uint32_t chunk, uint64_t chunk_limit, pps_hit* hits,
+                                                         uint64_t chunk_limit, pps_hit* hits,
                                                          uint32_t* hit_count, uint32_t hit_cap) {
   __shared__ uint32_t q_ent[BW_THREADS / 32][BQ_CAP];
   __shared__ uint64_t q_p[BW_THREADS / 32][32];
@@ -472,8 +479,8 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
     const uint32_t s = chunk_seg[c];
     const uint32_t job = T->batch[T->seg[s].batch].job;
     const BJob J = jobs[job];
-    const uint32_t within = (uint32_t)(c - chunk_off[s]) * chunk;
-    const uint32_t count = min(chunk, seg_count[s] - within);
+    const uint32_t within = (uint32_t)(c - chunk_off[s]) * J.chunk;
+    const uint32_t count = min(J.chunk, seg_count[s] - within);
     const uint64_t first = (uint64_t)seg_off[s] + within;
     for (uint32_t r = 0; r < count; r += 32u) {
       const bool valid = r + lane < count;
@@ -572,7 +579,7 @@ int ensure_state(pps_engine* e, size_t njobs) {
 }
 
 // The fixed per-wave launch sequence (everything reads counts from the tables).
-int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int chunk, int unroll, uint64_t chunk_limit,
+int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, uint64_t chunk_limit,
                 pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
   BatchState* b = e->batch;
   cudaStream_t st = e->st;
@@ -584,7 +591,7 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int chunk, i
   k_bscan<<<1, 1024, 0, st>>>(b->seg_count.p, b->seg_off.p, WAVE_SEGS, b->tot.p);
   k_bexpand<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, b->bitmap.p, b->seg_off.p, b->P.p, b->Pinv.p,
                                                   b->job_primes.p, b->job_sum.p, b->prime_cap);
-  k_bchunks<<<(WAVE_SEGS + 255) / 256, 256, 0, st>>>(b->tables.p, b->seg_count.p, b->chunk_count.p, chunk);
+  k_bchunks<<<(WAVE_SEGS + 255) / 256, 256, 0, st>>>(b->tables.p, b->jobs.p, b->seg_count.p, b->chunk_count.p);
   k_bscan<<<1, 1024, 0, st>>>(b->chunk_count.p, b->chunk_off.p, WAVE_SEGS, b->tot.p + 2);
   k_bchunkmap<<<WAVE_SEGS, 256, 0, st>>>(b->tables.p, b->chunk_count.p, b->chunk_off.p, b->chunk_seg.p,
                                          b->chunk_seg.n);
@@ -593,8 +600,8 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int chunk, i
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
   const int grid = (per_sm > 0 ? per_sm : 1) * e->num_sms;
   fn<<<grid, BW_THREADS, 0, st>>>(b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p,
-                                  b->chunk_seg.p, b->P.p, b->Pinv.p, b->tot.p, (uint32_t)chunk, chunk_limit, hits,
-                                  hit_count, hit_cap);
+                                  b->chunk_seg.p, b->P.p, b->Pinv.p, b->tot.p, chunk_limit, hits, hit_count,
+                                  hit_cap);
   CU(cudaGetLastError());
   e->launches += 10;
   return PPS_OK;
@@ -638,14 +645,26 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     J.win_mask = a.win_mask;
     J.qmax = jp.qmax;
     J.sign = jp.sign;
-    J.pad = 0;
+    J.chunk = 32;
     pmax_all = std::max(pmax_all, jp.pmax);
     qmax_all = std::max(qmax_all, std::min(jp.qmax, isqrt64(jp.pmax - 1)));
   }
   const uint32_t* dq = nullptr;
   BaseTable bt;
   if ((rc = prepare_sieving_primes(e, qmax_all, pmax_all, &dq, &bt))) return rc;
-  if (njobs) CU(cudaMemcpyAsync(b->jobs.p, hj.data(), njobs * sizeof(BJob), cudaMemcpyHostToDevice, e->st));
+  // Each job's chunk holds about `work` walk steps per lane, so a chunk of a
+  // short-n job and one of a long-n job take about the same time.
+  auto upload_jobs = [&](int work) -> int {
+    for (size_t j = 0; j < njobs; ++j) {
+      const uint64_t per = std::max<uint64_t>(1, hj[j].nsteps);
+      uint64_t c = ((uint64_t)work * 32u / per + 31u) & ~31ull;
+      hj[j].chunk = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 32), MAX_CHUNK);
+    }
+    // pageable source: the call returns once the table is staged, so hj may change afterwards
+    if (njobs) CU(cudaMemcpyAsync(b->jobs.p, hj.data(), njobs * sizeof(BJob), cudaMemcpyHostToDevice, e->st));
+    return PPS_OK;
+  };
+  if ((rc = upload_jobs(b->tuned_work > 0 ? b->tuned_work : 1024))) return rc;
   CU(cudaMemsetAsync(b->job_primes.p, 0, njobs * sizeof(unsigned long long), e->st));
   CU(cudaMemsetAsync(b->job_sum.p, 0, njobs * sizeof(unsigned long long), e->st));
   CU(cudaMemsetAsync(b->counters.p, 0, 4 * sizeof(uint32_t), e->st));
@@ -681,7 +700,7 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
   auto nseg_of = [](const BBatch& B) { return (uint32_t)((B.nbits + SEG_BITS - 1) / SEG_BITS); };
   size_t next = 0;
   int waves = 0;
-  bool tuned = b->tuned_chunk > 0;
+  bool tuned = b->tuned_work > 0;
   while (next < all.size()) {
     WaveTables* T = b->h_tables;
     CU(cudaEventSynchronize(b->copied));  // staging free again
@@ -709,16 +728,18 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     CU(cudaEventRecord(b->copied, e->st));
 
     if (!tuned) {
-      // time each (chunk, unroll) on the first 2% of this wave's chunks
-      const int chunks[] = {32, 64, 128};
+      // time each (work per chunk, unroll) on the first chunks of this wave,
+      // the same number of walk steps for every candidate
+      const int works[] = {256, 1024, 4096};
       const int unrolls[] = {8, 16};
       float best = 1e30f;
-      for (int c : chunks)
+      for (int w : works)
         for (int u : unrolls) {
+          if ((rc = upload_jobs(w))) return rc;
           CU(cudaMemsetAsync(b->counters.p + 2, 0, sizeof(uint32_t), e->st));
-          // tuning hits go to the survivors' buffer tail, then are dropped
-          const uint64_t lim = std::max<uint64_t>(64, (uint64_t)nseg * 4);
-          if ((rc = launch_wave(e, dq, bt.nq, c, u, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n)))
+          // tuning hits go to the survivors' buffer (its count is reset), then are dropped
+          const uint64_t lim = std::max<uint64_t>(16, (uint64_t)nseg * 4096 / (uint64_t)w);
+          if ((rc = launch_wave(e, dq, bt.nq, u, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n)))
             return rc;
           CU(cudaEventRecord(e->ev[0], e->st));
           CU(cudaMemsetAsync(b->tot.p + 3, 0, sizeof(uint64_t), e->st));
@@ -727,17 +748,25 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
           fn<<<std::max(per_sm, 1) * e->num_sms, BW_THREADS, 0, e->st>>>(
               b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->chunk_seg.p, b->P.p,
-              b->Pinv.p, b->tot.p, (uint32_t)c, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
+              b->Pinv.p, b->tot.p, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
           CU(cudaEventRecord(e->ev[1], e->st));
           CU(cudaEventSynchronize(e->ev[1]));
           float ms = 0;
           CU(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
-          if (ms < best) {
-            best = ms;
-            b->tuned_chunk = c;
+          // steps timed: the chunks walked (the wave may hold fewer than lim), each
+          // with the chunk size of the wave's first job, whose primes come first
+          uint64_t nch = 0;
+          CU(cudaMemcpy(&nch, b->tot.p + 2, sizeof nch, cudaMemcpyDeviceToHost));
+          const BJob& J0 = hj[T->batch[0].job];
+          const double steps = (double)std::min<uint64_t>(lim, nch) * J0.chunk * std::max<uint32_t>(J0.nsteps, 1);
+          const float per_step = (float)(ms / std::max(steps, 1.0));
+          if (per_step < best) {
+            best = per_step;
+            b->tuned_work = w;
             b->tuned_unroll = u;
           }
         }
+      if ((rc = upload_jobs(b->tuned_work))) return rc;
       // the tuning waves added to the per-job prime counts: clear them
       CU(cudaMemsetAsync(b->job_primes.p, 0, njobs * sizeof(unsigned long long), e->st));
       CU(cudaMemsetAsync(b->job_sum.p, 0, njobs * sizeof(unsigned long long), e->st));
@@ -745,14 +774,14 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
       tuned = true;
     }
     // the wave itself: a captured graph of the fixed sequence, replayed
-    if (!b->graph || b->graph_chunk != b->tuned_chunk || b->graph_unroll != b->tuned_unroll ||
+    if (!b->graph || b->graph_unroll != b->tuned_unroll ||
         b->graph_q != dq || b->graph_nq != bt.nq) {
       if (b->graph) cudaGraphExecDestroy(b->graph);
       b->graph = nullptr;
       cudaGraph_t g;
       CU(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
       const uint64_t launches0 = e->launches;
-      rc = launch_wave(e, dq, bt.nq, b->tuned_chunk, b->tuned_unroll, 0, b->hits.p, b->counters.p,
+      rc = launch_wave(e, dq, bt.nq, b->tuned_unroll, 0, b->hits.p, b->counters.p,
                        (uint32_t)b->hits.n);
       cudaError_t ce = cudaStreamEndCapture(e->st, &g);
       e->launches = launches0;
@@ -761,7 +790,6 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
       ce = cudaGraphInstantiate(&b->graph, g, 0);
       cudaGraphDestroy(g);
       if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-      b->graph_chunk = b->tuned_chunk;
       b->graph_unroll = b->tuned_unroll;
       b->graph_q = dq;
       b->graph_nq = bt.nq;
@@ -834,7 +862,7 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     bst->raw_hits = raw;
     bst->factors = nf;
     bst->waves = (uint32_t)waves;
-    bst->chunk = (uint32_t)b->tuned_chunk;
+    bst->chunk = (uint32_t)b->tuned_work;
     bst->unroll = (uint32_t)b->tuned_unroll;
     float ms = 0, fms = 0;
     CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[5]));

@@ -33,7 +33,7 @@ def test_batch_equals_single_jobs_mixed(pps, engine):
         assert int(pr[j]) == wst.primes and int(sm[j]) == wst.prime_sum, (j, meta[j])
         total += len(want)
     assert st.factors == total
-    assert st.waves >= 1 and st.chunk in (32, 64, 128) and st.unroll in (8, 16)
+    assert st.waves >= 1 and st.chunk in (256, 1024, 4096) and st.unroll in (8, 16)
 
 
 def test_batch_repeat_and_degenerate(pps, engine, ora):
