@@ -42,6 +42,9 @@ struct BJob {
   uint32_t proth, win_hi, win_mask, qmax;
   int32_t sign;
   uint32_t chunk;  // primes per work chunk: about the same walk steps for every job
+  // win_sh < 32: the small-p window, K < 2^win_sh or the low bits in win_mask
+  // all zero; 32: K < (win_hi + 1) * 2^32 or the low bits in win_mask zero
+  uint32_t win_sh, pad;
 };
 
 struct BBatch {
@@ -376,7 +379,7 @@ __device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t pl
 // One round: every lane walks one prime of the same job; flagged blocks of U
 // steps (and the partial last block) go to the warp's queue and are re-checked
 // exactly once the round's walks are done.
-template <bool S32, int U>
+template <bool S32, int U, bool WSH>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
                                         uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
                                         uint32_t* hit_count, uint32_t hit_cap) {
@@ -390,12 +393,17 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
     const uint64_t x = inv_pow2(J.nmin, p, ps);
     const uint64_t K = J.proth ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
-    const uint32_t win_hi = J.win_hi, win_mask = J.win_mask;
+    const uint32_t win_hi = J.win_hi, win_mask = J.win_mask, win_sh = J.win_sh;
     for (uint32_t b = 0; b < full; ++b) {
       bool f = false;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
+        // exact superset of the hits: a hit K = k*2^i with k < 2^kb is either
+        // below the window or has its low (window - kb + 1) bits zero
+        if (WSH)
+          f |= (__funnelshift_rc(klo, khi, win_sh) == 0u) | ((klo & win_mask) == 0u);
+        else
+          f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
         b_step<S32>(klo, khi, plo, phi, pinv_s, s);
       }
       if (f) {
@@ -486,12 +494,21 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
       const bool valid = r + lane < count;
       const uint64_t pi = first + r + (valid ? lane : 0u);
       const uint64_t p = P[pi], ps = Pinv[pi];
-      if (J.step == 32)
-        b_round<true, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, hit_count,
-                         hit_cap);
-      else
-        b_round<false, U>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, hit_count,
-                          hit_cap);
+      if (J.step == 32) {
+        if (J.win_sh < 32u)
+          b_round<true, U, true>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
+                                 hit_count, hit_cap);
+        else
+          b_round<true, U, false>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
+                                  hit_count, hit_cap);
+      } else {
+        if (J.win_sh < 32u)
+          b_round<false, U, true>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
+                                  hit_count, hit_cap);
+        else
+          b_round<false, U, false>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
+                                   hit_count, hit_cap);
+      }
     }
   }
 }
@@ -607,6 +624,27 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, 
   return PPS_OK;
 }
 
+int floor_lg2(uint64_t x) { return 63 - __builtin_clzll(x | 1ull); }
+
+// The one-job window tests K < 2^(32+u) with u >= 0; when p is below about
+// 2^(64-kb) (kmax < 2^kb) that bound passes most steps.  There the window is
+// placed at t = (lg p + kb - 1) / 2, which balances P(K < 2^t) ~ 2^(t - lg p)
+// against P(low t+1-kb bits zero) = 2^-(t+1-kb).  It stays exact while
+// K < p <= 2^(t+32), so that the funnel shift sees all of K >> t.
+void small_p_window(const pps_job_params& jp, BJob* J) {
+  J->win_sh = 32;
+  const int kb = floor_lg2(jp.kmax) + 1;
+  const int lp = floor_lg2(jp.pmin);
+  if (lp + kb - 64 >= 0) return;
+  const int B = floor_lg2(jp.pmax - 1) + 1;  // every p, and so every K, is below 2^B
+  int t = (lp + kb - 1) / 2;
+  t = std::max(t, B - 32);
+  t = std::max(t, kb);
+  if (t >= 32) return;
+  J->win_sh = (uint32_t)t;
+  J->win_mask = (1u << (t + 1 - kb)) - 1u;
+}
+
 }  // namespace
 
 extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t njobs, pps_factor* out,
@@ -646,6 +684,7 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     J.qmax = jp.qmax;
     J.sign = jp.sign;
     J.chunk = 32;
+    small_p_window(jp, &J);
     pmax_all = std::max(pmax_all, jp.pmax);
     qmax_all = std::max(qmax_all, std::min(jp.qmax, isqrt64(jp.pmax - 1)));
   }
