@@ -79,7 +79,10 @@ struct BatchState {
   DevBuf<uint64_t> tot;         // [0] primes, [1] sum, [2] chunks, [3] work counter
   DevBuf<unsigned long long> job_primes, job_sum;
   DevBuf<pps_hit> hits, out;
-  DevBuf<uint32_t> counters;    // [0] raw, [1] survivors
+  DevBuf<uint32_t> counters;    // [0] raw, [1] survivors, [2] tuning hits, [3] large-sieve items
+  DevBuf<uint64_t> qm;          // Barrett constants of the sieving primes
+  const uint32_t* qm_q = nullptr;  // sieving-prime table the constants belong to
+  uint32_t qm_n = 0;
   uint64_t prime_cap = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_unroll = 0;
@@ -161,20 +164,54 @@ __device__ __forceinline__ uint64_t b_first_odd_multiple(uint64_t q, uint64_t lo
   return st;
 }
 
-// large sieving primes of batch blockIdx.y into the wave bitmap
-__global__ void k_bsieve_large(const uint8_t* tables, const uint32_t* q, uint32_t* bitmap) {
+// Barrett constants of the sieving primes: m = floor((2^64 - 1) / q), which is
+// floor(2^64 / q) for every odd q > 1 (Barrett, CRYPTO '86).
+__global__ void k_brecip(const uint32_t* q, uint32_t nq, uint64_t* m) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x)
+    m[i] = ~0ull / (uint64_t)q[i];
+}
+
+// x mod q from the Barrett constant: the estimate umulhi(x, m) is at most 2
+// below floor(x / q), so at most two corrections.
+__device__ __forceinline__ uint64_t b_mod(uint64_t x, uint64_t q, uint64_t m) {
+  uint64_t r = x - __umul64hi(x, m) * q;
+  if (r >= q) r -= q;
+  if (r >= q) r -= q;
+  return r;
+}
+
+constexpr uint32_t LARGE_SLICES = 64;  // work items per batch in the large-prime pass
+
+// Large sieving primes (q >= SEG_BITS) into the wave bitmap.  Work items are
+// (batch, slice) pairs taken from a device counter, so a wave of a few wide
+// batches and one of many narrow batches both fill the GPU.
+__global__ void k_bsieve_large(const uint8_t* tables, const uint32_t* q, const uint64_t* qm, uint32_t* bitmap,
+                               uint32_t* item_counter) {
+  __shared__ uint32_t s_item;
   const WaveTables* T = wt(tables);
-  const uint32_t b = blockIdx.y;
-  if (b >= T->nbatch) return;
-  const BBatch B = T->batch[b];
-  if (B.nq <= B.nq_seg) return;
-  uint32_t* bm = bitmap + (size_t)B.seg0 * SEG_WORDS;
-  const uint64_t hi = B.lo + 2ull * B.nbits;
-  for (uint32_t i = B.nq_seg + blockIdx.x * blockDim.x + threadIdx.x; i < B.nq; i += gridDim.x * blockDim.x) {
-    const uint64_t qq = q[i];
-    if (qq * qq >= hi) continue;
-    const uint64_t st = b_first_odd_multiple(qq, B.lo);
-    for (uint64_t j = (st - B.lo) >> 1; j < B.nbits; j += qq) atomicAnd(&bm[j >> 5], ~(1u << (j & 31u)));
+  const uint32_t nitems = T->nbatch * LARGE_SLICES;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(item_counter, 1u);
+    __syncthreads();
+    const uint32_t item = s_item;
+    __syncthreads();
+    if (item >= nitems) return;
+    const BBatch B = T->batch[item / LARGE_SLICES];
+    const uint32_t slice = item % LARGE_SLICES;
+    if (B.nq <= B.nq_seg) continue;
+    uint32_t* bm = bitmap + (size_t)B.seg0 * SEG_WORDS;
+    const uint64_t hi = B.lo + 2ull * B.nbits;
+    for (uint32_t i = B.nq_seg + slice * blockDim.x + threadIdx.x; i < B.nq; i += LARGE_SLICES * blockDim.x) {
+      const uint64_t qq = q[i];
+      if (qq * qq >= hi) continue;
+      uint64_t st = qq * qq;
+      if (st < B.lo) {
+        const uint64_t r = b_mod(B.lo, qq, qm[i]);
+        st = r ? B.lo + (qq - r) : B.lo;
+        if ((st & 1ull) == 0ull) st += qq;
+      }
+      for (uint64_t j = (st - B.lo) >> 1; j < B.nbits; j += qq) atomicAnd(&bm[j >> 5], ~(1u << (j & 31u)));
+    }
   }
 }
 
@@ -603,7 +640,8 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, 
   CU(cudaMemsetAsync(b->bitmap.p, 0xff, (size_t)WAVE_SEGS * SEG_WORDS * 4, st));
   CU(cudaMemsetAsync(b->tot.p, 0, 4 * sizeof(uint64_t), st));
   k_bcounts<<<(WAVE_BATCHES + 255) / 256, 256, 0, st>>>(b->tables.p, dq, nq_all);
-  k_bsieve_large<<<dim3(8, WAVE_BATCHES), 256, 0, st>>>(b->tables.p, dq, b->bitmap.p);
+  CU(cudaMemsetAsync(b->counters.p + 3, 0, sizeof(uint32_t), st));
+  k_bsieve_large<<<e->num_sms * 8, 256, 0, st>>>(b->tables.p, dq, b->qm.p, b->bitmap.p, b->counters.p + 3);
   k_bsieve_seg<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, dq, b->bitmap.p, b->seg_count.p);
   k_bscan<<<1, 1024, 0, st>>>(b->seg_count.p, b->seg_off.p, WAVE_SEGS, b->tot.p);
   k_bexpand<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, b->bitmap.p, b->seg_off.p, b->P.p, b->Pinv.p,
@@ -620,7 +658,7 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, 
                                   b->chunk_seg.p, b->P.p, b->Pinv.p, b->tot.p, chunk_limit, hits, hit_count,
                                   hit_cap);
   CU(cudaGetLastError());
-  e->launches += 10;
+  e->launches += 9;  // the kernels above, each once
   return PPS_OK;
 }
 
@@ -691,6 +729,17 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
   const uint32_t* dq = nullptr;
   BaseTable bt;
   if ((rc = prepare_sieving_primes(e, qmax_all, pmax_all, &dq, &bt))) return rc;
+  if (b->qm_q != dq || b->qm_n != bt.nq) {
+    // a new sieving-prime table: its Barrett constants (the graph is recaptured too)
+    if ((rc = b->qm.ensure(std::max<uint32_t>(bt.nq, 1)))) return rc;
+    if (bt.nq) {
+      k_brecip<<<std::min<uint32_t>((bt.nq + 255) / 256, 4096), 256, 0, e->st>>>(dq, bt.nq, b->qm.p);
+      CU(cudaGetLastError());
+      e->launches++;
+    }
+    b->qm_q = dq;
+    b->qm_n = bt.nq;
+  }
   // Each job's chunk holds about `work` walk steps per lane, so a chunk of a
   // short-n job and one of a long-n job take about the same time.
   auto upload_jobs = [&](int work) -> int {
