@@ -112,11 +112,13 @@ class Clocks:
 
 
 def _traffic_from_profile() -> float | None:
-    f = ROOT / "profiles" / "walk_c2_ncu.md"
+    """DRAM bytes per prime of the walk kernel from the committed ncu summary
+    (the walk reads each prime's 16 B once, whatever the n range)."""
+    f = ROOT / "profiles" / "k_walk32q_c2.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_step_of_one_prime:"):
+        if line.startswith("dram_bytes_per_prime:"):
             return float(line.split(":")[1])
     return None
 
@@ -327,11 +329,14 @@ def run_gpu(args) -> None:
     peaks = _measured_peaks()
     hbm = peaks.get("hbm_gbs")
     sieve_gbs = 16.0 * primes / (sieve_ms * 1e-3) / 1e9 if sieve_ms > 0 else None
-    launches_walk = len(stats)
+    launches_walk = len(stats)  # one walk launch per job
+    variant = stats[-1].variant if stats else 0
     roofline = {"bound": "imad", "achieved": achieved / 1e9, "peak": peak_mults / 1e9,
                 "unit": "Gmul/s", "frac": achieved / peak_mults,
-                "traffic": (traffic * steps_done / launches_walk) if traffic else None,
-                "kernel": "k_walk", "peak_source": "measured in this run (pps_measure_imad_peak)",
+                "traffic": (traffic * primes / launches_walk) if traffic else None,
+                "traffic_unit": "bytes per launch (ncu DRAM bytes per prime x primes per launch)",
+                "kernel": f"{'k_walk32q' if variant >= 10 else 'k_walk'} (variant {variant})",
+                "peak_source": "measured in this run (pps_measure_imad_peak)",
                 "work_per_unit": "3 multiplies per walk step (one prime advanced by 32 n)",
                 "sieve": {"bound": "hbm", "achieved": sieve_gbs, "peak": hbm, "unit": "GB/s",
                           "frac": (sieve_gbs / hbm) if (sieve_gbs and hbm) else None,
