@@ -187,6 +187,64 @@ int pps_run_batch(pps_engine *e, const pps_job_params *jobs, size_t njobs, pps_f
 /* Per-job prime count and wrapping prime sum of the last pps_run_batch. */
 int pps_batch_job_primes(pps_engine *e, size_t njobs, uint64_t *primes, uint64_t *sums);
 
+/* ---- Serving loop (no counterpart in the reference, which runs one range per
+   process, main.c:887-1266): continuous batching over the batched form.  A
+   worker thread owns an engine on `device`; each turn it admits queued jobs,
+   runs one wave over the next p pieces of every admitted job (one piece per
+   job first, oldest first, then the oldest fill the wave), and finishes the
+   jobs whose last piece was in it.  Jobs join at the next wave.  Admission is
+   in submission order, while a job slot is free (max_jobs) and the reserved
+   candidate-buffer bytes stay within factor_bytes: a job reserves twice its
+   expected raw candidates (32 B each, Mertens estimate #k * #n * ln(ln pmax /
+   ln pmin)), at least 16 KiB; a job whose reservation alone exceeds the budget
+   is refused at submission with PPS_ERR_INSUFFICIENT_RESOURCE.  Job state
+   between waves (parameters, prime counters) stays in device slots.  Each
+   job's factor list is exactly what pps_run_job returns for it alone. */
+typedef struct pps_server pps_server;
+
+typedef struct {
+  uint64_t factor_bytes;   /* candidate-buffer budget; 0 = 1 GiB */
+  uint32_t max_jobs;       /* admitted jobs at once (device slots); 0 = 4096, at most 65536 */
+  uint32_t wave_segments;  /* sieve segments (2^18 odd candidates) per wave; 0 = the maximum, 16384 */
+} pps_server_config;
+
+#define PPS_JOB_QUEUED  0  /* submitted, waiting for admission */
+#define PPS_JOB_RUNNING 1  /* admitted: its pieces are being walked */
+#define PPS_JOB_DONE    2
+#define PPS_JOB_FAILED  3
+
+typedef struct {
+  uint64_t primes, prime_sum, factors;
+  double latency_ms;       /* submission to result ready */
+  int32_t status;          /* PPS_OK, or the failure code of a failed job */
+  int32_t pad;
+} pps_job_result;
+
+typedef struct {
+  uint64_t submitted, admitted, completed, refused, failed;
+  uint64_t queued, running, reserved_bytes;
+  uint64_t primes, steps, waves;
+  uint32_t chunk, unroll;  /* the walk tuning of the batched form */
+  double busy_ms;          /* worker time inside waves */
+  double p50_ms, p99_ms;   /* latency of the completed jobs (nearest rank) */
+} pps_server_stats;
+
+int pps_server_create(int device, const pps_server_config *cfg, pps_server **out);
+/* Stops the worker after its current wave; unfinished jobs are dropped.  No
+   other call on this server may be in progress or follow. */
+int pps_server_destroy(pps_server *s);
+/* jp: normalised (pps_normalize).  *id identifies the job until its result is taken. */
+int pps_job_submit(pps_server *s, const pps_job_params *jp, uint64_t *id);
+int pps_job_poll(pps_server *s, uint64_t id, int *state);
+/* Waits up to timeout_s seconds (< 0: no limit; PPS_ERR_TIMEOUT when it
+   expires).  Then *nout = the factor count and res (if given) the job's
+   figures.  With out == NULL the job stays (a size query); otherwise the
+   sorted (p, k, n, c) list is copied (PPS_ERR_OVERFLOW, job kept, when cap is
+   too small) and the job is released.  A failed job returns its failure code. */
+int pps_job_wait(pps_server *s, uint64_t id, double timeout_s, pps_factor *out, size_t cap,
+                 size_t *nout, pps_job_result *res);
+int pps_server_get_stats(pps_server *s, pps_server_stats *st);
+
 /* Allocation-free walk (no counterpart in the reference): the walk and the
    output rule over np primes already in device memory (d_P), factors written
    to the caller's device buffer d_out (capacity out_cap, in no particular

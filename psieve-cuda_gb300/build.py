@@ -75,7 +75,7 @@ def build(verbose: bool = False) -> dict[str, Path]:
     lib = OUT / "libppsgpu.so"
     lib_objs = [objs[s] for s in LIB_SOURCES if s in objs]
     if _stale(lib, lib_objs):
-        _run([nv, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lcudart"])
+        _run([nv, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lcudart", "-lpthread"])
     out = {"libppsgpu": lib}
 
     compat_objs = [objs[s] for s in COMPAT_SOURCES if s in objs]

@@ -10,8 +10,9 @@
 // wave after the wave's tables are copied in.  The walk kernel's warps pop
 // chunks of CHUNK primes (all of one job, so every lane of a warp has the same
 // n loop) from a device counter until the wave is exhausted.  Raw candidates
-// carry their job id; one filter launch after the last wave applies each
-// job's output rule.
+// carry their job slot; a filter launch after each wave applies each job's
+// output rule.  Jobs live in device slots (parameters, prime counters), so the
+// serving loop can admit and retire jobs between waves.
 //
 // Reference counterpart: none in one piece -- the reference runs one range per
 // process (main.c:887-1266) and one kernel per n slice (pps/appcu.cu:1194-1261).
@@ -90,6 +91,9 @@ struct BatchState {
   uint32_t graph_nq = 0;
   cudaEvent_t copied = nullptr;
   int tuned_work = 0, tuned_unroll = 0;  // walk steps per chunk (x32 lanes), inner unroll
+  std::vector<BJob> hjobs;               // host mirror of the device job slots
+  std::vector<uint64_t> slot_pmax;       // each slot's pmax (sieving-prime bound)
+  DevBuf<unsigned long long> bak_primes, bak_sum;  // slot counters before a wave
 };
 
 void batch_state_free(pps_engine* e) {
@@ -114,6 +118,9 @@ void batch_state_free(pps_engine* e) {
   b->hits.release();
   b->out.release();
   b->counters.release();
+  b->qm.release();
+  b->bak_primes.release();
+  b->bak_sum.release();
   delete b;
   e->batch = nullptr;
 }
@@ -596,11 +603,7 @@ __global__ void k_bfilter(const pps_hit* hits, const uint32_t* d_nhits, uint32_t
 
 namespace {
 
-struct BatchPlan {
-  std::vector<BBatch> batches;  // in wave order
-};
-
-int ensure_state(pps_engine* e, size_t njobs) {
+int ensure_state(pps_engine* e) {
   if (!e->batch) e->batch = new BatchState();
   BatchState* b = e->batch;
   int rc;
@@ -622,13 +625,17 @@ int ensure_state(pps_engine* e, size_t njobs) {
     if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
     if (cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming) != cudaSuccess)
       return set_err(PPS_ERR_CUDA, "event");
-    // job tables at their maximum size once: the captured graph holds these pointers
+    // job slots at their maximum size once: the captured graph holds these pointers
     if ((rc = b->jobs.ensure(MAX_JOBS)) || (rc = b->job_primes.ensure(MAX_JOBS)) ||
-        (rc = b->job_sum.ensure(MAX_JOBS)))
+        (rc = b->job_sum.ensure(MAX_JOBS)) || (rc = b->bak_primes.ensure(MAX_JOBS)) ||
+        (rc = b->bak_sum.ensure(MAX_JOBS)))
       return rc;
+    CU(cudaMemsetAsync(b->jobs.p, 0, MAX_JOBS * sizeof(BJob), e->st));
+    CU(cudaMemsetAsync(b->counters.p, 0, 4 * sizeof(uint32_t), e->st));
+    b->hjobs.assign(MAX_JOBS, BJob{});
+    b->slot_pmax.assign(MAX_JOBS, 0);
     b->ready = true;
   }
-  (void)njobs;
   return PPS_OK;
 }
 
@@ -683,195 +690,267 @@ void small_p_window(const pps_job_params& jp, BJob* J) {
   J->win_mask = (1u << (t + 1 - kb)) - 1u;
 }
 
+BJob make_job(const pps_job_params& jp) {
+  WalkArgs a;
+  walk_args_for_job(&jp, &a);
+  BJob J;
+  memset(&J, 0, sizeof J);
+  J.kmin = jp.kmin;
+  J.kmax = jp.kmax;
+  J.kstep = jp.kstep;
+  J.koffset = jp.koffset;
+  J.nmin = jp.nmin;
+  J.nmax = jp.nmax;
+  J.step = jp.step;
+  J.nsteps = a.nsteps;
+  J.proth = a.proth;
+  J.win_hi = a.win_hi;
+  J.win_mask = a.win_mask;
+  J.qmax = jp.qmax;
+  J.sign = jp.sign;
+  J.chunk = 32;
+  small_p_window(jp, &J);
+  return J;
+}
+
+// Each job's chunk holds about `work` walk steps per lane, so a chunk of a
+// short-n job and one of a long-n job take about the same time.
+uint32_t chunk_for(const BJob& J, int work) {
+  const uint64_t per = std::max<uint64_t>(1, J.nsteps);
+  const uint64_t c = ((uint64_t)work * 32u / per + 31u) & ~31ull;
+  return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 32), MAX_CHUNK);
+}
+
+// Copy mirror slots [lo, hi) to the device.  The source is pageable: the call
+// returns once it is staged, so the mirror may change right afterwards.
+int upload_slots(pps_engine* e, uint32_t lo, uint32_t hi) {
+  BatchState* b = e->batch;
+  if (hi > lo)
+    CU(cudaMemcpyAsync(b->jobs.p + lo, b->hjobs.data() + lo, (size_t)(hi - lo) * sizeof(BJob),
+                       cudaMemcpyHostToDevice, e->st));
+  return PPS_OK;
+}
+
+// Chunk sizes of slots [lo, hi] for a work target; uploads what changed.
+int set_chunks(pps_engine* e, uint32_t lo, uint32_t hi, int work) {
+  BatchState* b = e->batch;
+  bool changed = false;
+  for (uint32_t s = lo; s <= hi; ++s) {
+    if (!b->slot_pmax[s]) continue;
+    const uint32_t c = chunk_for(b->hjobs[s], work);
+    if (c != b->hjobs[s].chunk) {
+      b->hjobs[s].chunk = c;
+      changed = true;
+    }
+  }
+  return changed ? upload_slots(e, lo, hi + 1) : PPS_OK;
+}
+
 }  // namespace
 
-extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t njobs, pps_factor* out,
-                             size_t cap, size_t* nout, size_t* job_offsets, pps_batch_stats* bst) {
-  if (!e || (!jobs && njobs)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
-  if (njobs > MAX_JOBS) return set_err(PPS_ERR_INVALID_PARAM, "at most %u jobs per batch", MAX_JOBS);
-  for (size_t j = 0; j < njobs; ++j)
-    if (jobs[j].step < 1 || jobs[j].step > 32 || jobs[j].pmin <= (1ull << 32))
-      return set_err(PPS_ERR_INVALID_PARAM, "job %zu not normalized", j);
-  CU(cudaSetDevice(e->device));
-  int rc;
-  if ((rc = ensure_state(e, njobs ? njobs : 1))) return rc;
-  BatchState* b = e->batch;
-  if (bst) memset(bst, 0, sizeof *bst);
-  CU(cudaEventRecord(e->ev[6], e->st));
+uint32_t batch_max_slots() { return MAX_JOBS; }
+uint64_t batch_wave_segments() { return WAVE_SEGS; }
+uint64_t batch_max_piece_span() { return 2ull * SEG_BITS * BATCH_SEGS; }
+uint64_t batch_piece_segments(uint64_t lo, uint64_t hi) {
+  const uint64_t lo0 = lo | 1ull;
+  if (hi <= lo0) return 0;
+  const uint64_t span = batch_max_piece_span(), bits = (hi - lo0 + 1) / 2;
+  // whole batches of BATCH_SEGS segments, then the remainder
+  const uint64_t full = (hi - lo0) / span;
+  const uint64_t rest = bits - full * (span / 2);
+  return full * BATCH_SEGS + (rest + SEG_BITS - 1) / SEG_BITS;
+}
 
-  // job table and the sieving-prime table for the largest p of the batch
-  std::vector<BJob> hj(njobs);
-  uint64_t pmax_all = 5;
-  uint32_t qmax_all = 3;
-  for (size_t j = 0; j < njobs; ++j) {
-    const pps_job_params& jp = jobs[j];
-    WalkArgs a;
-    walk_args_for_job(&jp, &a);
-    BJob& J = hj[j];
-    J.kmin = jp.kmin;
-    J.kmax = jp.kmax;
-    J.kstep = jp.kstep;
-    J.koffset = jp.koffset;
-    J.nmin = jp.nmin;
-    J.nmax = jp.nmax;
-    J.step = jp.step;
-    J.nsteps = a.nsteps;
-    J.proth = a.proth;
-    J.win_hi = a.win_hi;
-    J.win_mask = a.win_mask;
-    J.qmax = jp.qmax;
-    J.sign = jp.sign;
-    J.chunk = 32;
-    small_p_window(jp, &J);
-    pmax_all = std::max(pmax_all, jp.pmax);
-    qmax_all = std::max(qmax_all, std::min(jp.qmax, isqrt64(jp.pmax - 1)));
+int batch_prepare(pps_engine* e) {
+  if (!e) return set_err(PPS_ERR_INVALID_PARAM, "null engine");
+  CU(cudaSetDevice(e->device));
+  return ensure_state(e);
+}
+
+void batch_tuning(pps_engine* e, uint32_t* work, uint32_t* unroll) {
+  const BatchState* b = e ? e->batch : nullptr;
+  if (work) *work = b ? (uint32_t)b->tuned_work : 0;
+  if (unroll) *unroll = b ? (uint32_t)b->tuned_unroll : 0;
+}
+
+int batch_set_jobs(pps_engine* e, uint32_t slot0, const pps_job_params* jobs, size_t n) {
+  int rc;
+  if ((rc = batch_prepare(e))) return rc;
+  if (!jobs && n) return set_err(PPS_ERR_INVALID_PARAM, "null jobs");
+  if ((uint64_t)slot0 + n > MAX_JOBS) return set_err(PPS_ERR_INVALID_PARAM, "at most %u job slots", MAX_JOBS);
+  for (size_t j = 0; j < n; ++j)
+    if (jobs[j].step < 1 || jobs[j].step > 32 || jobs[j].pmin <= (1ull << 32) || jobs[j].pmax <= jobs[j].pmin)
+      return set_err(PPS_ERR_INVALID_PARAM, "job %zu not normalized", j);
+  BatchState* b = e->batch;
+  const int work = b->tuned_work > 0 ? b->tuned_work : 1024;
+  for (size_t j = 0; j < n; ++j) {
+    BJob J = make_job(jobs[j]);
+    J.chunk = chunk_for(J, work);
+    b->hjobs[slot0 + j] = J;
+    b->slot_pmax[slot0 + j] = jobs[j].pmax;
   }
+  if ((rc = upload_slots(e, slot0, (uint32_t)(slot0 + n)))) return rc;
+  if (n) {
+    CU(cudaMemsetAsync(b->job_primes.p + slot0, 0, n * sizeof(unsigned long long), e->st));
+    CU(cudaMemsetAsync(b->job_sum.p + slot0, 0, n * sizeof(unsigned long long), e->st));
+  }
+  return PPS_OK;
+}
+
+int batch_job_counts(pps_engine* e, uint32_t slot0, size_t n, uint64_t* primes, uint64_t* sums) {
+  int rc;
+  if ((rc = batch_prepare(e))) return rc;
+  if ((uint64_t)slot0 + n > MAX_JOBS) return set_err(PPS_ERR_INVALID_PARAM, "slot range");
+  BatchState* b = e->batch;
+  CU(cudaStreamSynchronize(e->st));
+  if (primes && n) CU(cudaMemcpy(primes, b->job_primes.p + slot0, n * 8, cudaMemcpyDeviceToHost));
+  if (sums && n) CU(cudaMemcpy(sums, b->job_sum.p + slot0, n * 8, cudaMemcpyDeviceToHost));
+  return PPS_OK;
+}
+
+int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pps_hit>* survivors,
+               uint64_t* raw_hits, double* filter_ms) {
+  int rc;
+  if ((rc = batch_prepare(e))) return rc;
+  if (!pieces && n) return set_err(PPS_ERR_INVALID_PARAM, "null pieces");
+  if (n == 0) return PPS_OK;
+  BatchState* b = e->batch;
+  cudaStream_t st = e->st;
+
+  // the pieces' slots, and the sieving bound over them
+  uint32_t smin = MAX_JOBS, smax = 0;
+  uint64_t need_q = SEG_BITS;
+  for (size_t i = 0; i < n; ++i) {
+    const BatchPiece& pc = pieces[i];
+    if (pc.slot >= MAX_JOBS || !b->slot_pmax[pc.slot] || pc.hi <= pc.lo || pc.hi > b->slot_pmax[pc.slot] ||
+        pc.lo <= (1ull << 32))
+      return set_err(PPS_ERR_INVALID_PARAM, "piece %zu: bad slot or range", i);
+    smin = std::min(smin, pc.slot);
+    smax = std::max(smax, pc.slot);
+    need_q = std::max<uint64_t>(need_q, std::min<uint64_t>(b->hjobs[pc.slot].qmax, isqrt64(pc.hi - 1)));
+  }
+  // The whole cached table of sieving primes serves the wave (each batch stops
+  // at its own limit on the device); it only grows, so the graph stays valid.
+  const uint32_t want = (uint32_t)std::max<uint64_t>(need_q, e->base_limit);
   const uint32_t* dq = nullptr;
   BaseTable bt;
-  if ((rc = prepare_sieving_primes(e, qmax_all, pmax_all, &dq, &bt))) return rc;
-  if (b->qm_q != dq || b->qm_n != bt.nq) {
+  if ((rc = prepare_sieving_primes(e, want, (uint64_t)want * want + 1, &dq, &bt))) return rc;
+  const uint32_t nq_all = e->base_count;
+  if (b->qm_q != dq || b->qm_n != nq_all) {
     // a new sieving-prime table: its Barrett constants (the graph is recaptured too)
-    if ((rc = b->qm.ensure(std::max<uint32_t>(bt.nq, 1)))) return rc;
-    if (bt.nq) {
-      k_brecip<<<std::min<uint32_t>((bt.nq + 255) / 256, 4096), 256, 0, e->st>>>(dq, bt.nq, b->qm.p);
+    if ((rc = b->qm.ensure(std::max<uint32_t>(nq_all, 1)))) return rc;
+    if (nq_all) {
+      k_brecip<<<std::min<uint32_t>((nq_all + 255) / 256, 4096), 256, 0, st>>>(dq, nq_all, b->qm.p);
       CU(cudaGetLastError());
       e->launches++;
     }
     b->qm_q = dq;
-    b->qm_n = bt.nq;
+    b->qm_n = nq_all;
   }
-  // Each job's chunk holds about `work` walk steps per lane, so a chunk of a
-  // short-n job and one of a long-n job take about the same time.
-  auto upload_jobs = [&](int work) -> int {
-    for (size_t j = 0; j < njobs; ++j) {
-      const uint64_t per = std::max<uint64_t>(1, hj[j].nsteps);
-      uint64_t c = ((uint64_t)work * 32u / per + 31u) & ~31ull;
-      hj[j].chunk = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 32), MAX_CHUNK);
-    }
-    // pageable source: the call returns once the table is staged, so hj may change afterwards
-    if (njobs) CU(cudaMemcpyAsync(b->jobs.p, hj.data(), njobs * sizeof(BJob), cudaMemcpyHostToDevice, e->st));
-    return PPS_OK;
-  };
-  if ((rc = upload_jobs(b->tuned_work > 0 ? b->tuned_work : 1024))) return rc;
-  CU(cudaMemsetAsync(b->job_primes.p, 0, njobs * sizeof(unsigned long long), e->st));
-  CU(cudaMemsetAsync(b->job_sum.p, 0, njobs * sizeof(unsigned long long), e->st));
-  CU(cudaMemsetAsync(b->counters.p, 0, 4 * sizeof(uint32_t), e->st));
 
-  // batches, most expensive jobs first (steps per prime x range width)
-  std::vector<size_t> order(njobs);
-  for (size_t j = 0; j < njobs; ++j) order[j] = j;
-  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
-    const double cx = (double)hj[x].nsteps * (double)(jobs[x].pmax - jobs[x].pmin);
-    const double cy = (double)hj[y].nsteps * (double)(jobs[y].pmax - jobs[y].pmin);
-    return cx > cy;
-  });
-  std::vector<BBatch> all;
-  for (size_t oi = 0; oi < njobs; ++oi) {
-    const size_t j = order[oi];
-    const pps_job_params& jp = jobs[j];
-    const uint64_t lo0 = jp.pmin | 1ull;
-    if (jp.pmax <= lo0) continue;
-    const uint64_t span = 2ull * SEG_BITS * BATCH_SEGS;
-    for (uint64_t lo = lo0; lo < jp.pmax; lo += span) {
-      const uint64_t hi = std::min(jp.pmax, lo + span);
+  // wave tables: each piece as batches of at most BATCH_SEGS segments
+  CU(cudaEventSynchronize(b->copied));  // staging free again
+  WaveTables* T = b->h_tables;
+  uint32_t nseg = 0, nb = 0;
+  const uint64_t span = batch_max_piece_span();
+  for (size_t i = 0; i < n; ++i) {
+    const BatchPiece& pc = pieces[i];
+    const BJob& J = b->hjobs[pc.slot];
+    for (uint64_t lo = pc.lo | 1ull; lo < pc.hi; lo += span) {
+      const uint64_t hi = std::min(pc.hi, lo + span);
       BBatch B;
       memset(&B, 0, sizeof B);
       B.lo = lo;
       B.nbits = (hi - lo + 1) / 2;
-      B.job = (uint32_t)j;
-      B.limit = std::min(jp.qmax, isqrt64(hi - 1));
-      all.push_back(B);
-    }
-  }
-
-  // walk tile choice: chunk size and unroll, timed on a sample of the first wave
-  auto nseg_of = [](const BBatch& B) { return (uint32_t)((B.nbits + SEG_BITS - 1) / SEG_BITS); };
-  size_t next = 0;
-  int waves = 0;
-  bool tuned = b->tuned_work > 0;
-  while (next < all.size()) {
-    WaveTables* T = b->h_tables;
-    CU(cudaEventSynchronize(b->copied));  // staging free again
-    uint32_t nseg = 0, nb = 0;
-    while (next < all.size() && nb < WAVE_BATCHES) {
-      BBatch B = all[next];
-      const uint32_t ns = nseg_of(B);
-      if (nseg + ns > WAVE_SEGS) break;
+      B.job = pc.slot;
+      B.limit = (uint32_t)std::min<uint64_t>(J.qmax, isqrt64(hi - 1));
+      const uint32_t ns = (uint32_t)((B.nbits + SEG_BITS - 1) / SEG_BITS);
+      if (nseg + ns > WAVE_SEGS || nb >= WAVE_BATCHES)
+        return set_err(PPS_ERR_INVALID_PARAM, "pieces exceed one wave (%u segments)", WAVE_SEGS);
       B.seg0 = nseg;
       for (uint32_t s = 0; s < ns; ++s) {
         BSeg& S = T->seg[nseg + s];
         S.lo = B.lo + 2ull * (uint64_t)s * SEG_BITS;
-        const uint64_t left = B.nbits - (uint64_t)s * SEG_BITS;
-        S.bits = (uint32_t)std::min<uint64_t>(left, SEG_BITS);
+        S.bits = (uint32_t)std::min<uint64_t>(B.nbits - (uint64_t)s * SEG_BITS, SEG_BITS);
         S.batch = nb;
       }
       T->batch[nb++] = B;
       nseg += ns;
-      ++next;
     }
-    T->nseg = nseg;
-    T->nbatch = nb;
-    const size_t bytes = offsetof(WaveTables, seg) + sizeof(BSeg) * WAVE_SEGS + sizeof(BBatch) * nb;
-    CU(cudaMemcpyAsync(b->tables.p, T, bytes, cudaMemcpyHostToDevice, e->st));
-    CU(cudaEventRecord(b->copied, e->st));
+  }
+  T->nseg = nseg;
+  T->nbatch = nb;
+  const size_t bytes = offsetof(WaveTables, seg) + sizeof(BSeg) * WAVE_SEGS + sizeof(BBatch) * nb;
+  CU(cudaMemcpyAsync(b->tables.p, T, bytes, cudaMemcpyHostToDevice, st));
+  CU(cudaEventRecord(b->copied, st));
 
-    if (!tuned) {
-      // time each (work per chunk, unroll) on the first chunks of this wave,
-      // the same number of walk steps for every candidate
-      const int works[] = {256, 1024, 4096};
-      const int unrolls[] = {8, 16};
-      float best = 1e30f;
-      for (int w : works)
-        for (int u : unrolls) {
-          if ((rc = upload_jobs(w))) return rc;
-          CU(cudaMemsetAsync(b->counters.p + 2, 0, sizeof(uint32_t), e->st));
-          // tuning hits go to the survivors' buffer (its count is reset), then are dropped
-          const uint64_t lim = std::max<uint64_t>(16, (uint64_t)nseg * 4096 / (uint64_t)w);
-          if ((rc = launch_wave(e, dq, bt.nq, u, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n)))
-            return rc;
-          CU(cudaEventRecord(e->ev[0], e->st));
-          CU(cudaMemsetAsync(b->tot.p + 3, 0, sizeof(uint64_t), e->st));
-          auto fn = u == 16 ? k_bwalk<16> : k_bwalk<8>;
-          int per_sm = 0;
-          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
-          fn<<<std::max(per_sm, 1) * e->num_sms, BW_THREADS, 0, e->st>>>(
-              b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->chunk_seg.p, b->P.p,
-              b->Pinv.p, b->tot.p, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
-          CU(cudaEventRecord(e->ev[1], e->st));
-          CU(cudaEventSynchronize(e->ev[1]));
-          float ms = 0;
-          CU(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
-          // steps timed: the chunks walked (the wave may hold fewer than lim), each
-          // with the chunk size of the wave's first job, whose primes come first
-          uint64_t nch = 0;
-          CU(cudaMemcpy(&nch, b->tot.p + 2, sizeof nch, cudaMemcpyDeviceToHost));
-          const BJob& J0 = hj[T->batch[0].job];
-          const double steps = (double)std::min<uint64_t>(lim, nch) * J0.chunk * std::max<uint32_t>(J0.nsteps, 1);
-          const float per_step = (float)(ms / std::max(steps, 1.0));
-          if (per_step < best) {
-            best = per_step;
-            b->tuned_work = w;
-            b->tuned_unroll = u;
-          }
+  // slot counters before the wave: the tuning runs and an overflow re-run put them back
+  const size_t nsl = (size_t)(smax - smin) + 1;
+  CU(cudaMemcpyAsync(b->bak_primes.p + smin, b->job_primes.p + smin, nsl * 8, cudaMemcpyDeviceToDevice, st));
+  CU(cudaMemcpyAsync(b->bak_sum.p + smin, b->job_sum.p + smin, nsl * 8, cudaMemcpyDeviceToDevice, st));
+  auto restore = [&]() -> int {
+    CU(cudaMemcpyAsync(b->job_primes.p + smin, b->bak_primes.p + smin, nsl * 8, cudaMemcpyDeviceToDevice, st));
+    CU(cudaMemcpyAsync(b->job_sum.p + smin, b->bak_sum.p + smin, nsl * 8, cudaMemcpyDeviceToDevice, st));
+    return PPS_OK;
+  };
+
+  if (!b->tuned_work) {
+    // time each (work per chunk, unroll) on the first chunks of this wave,
+    // the same number of walk steps for every candidate
+    const int works[] = {256, 1024, 4096};
+    const int unrolls[] = {8, 16};
+    float best = 1e30f;
+    for (int w : works)
+      for (int u : unrolls) {
+        if ((rc = set_chunks(e, smin, smax, w))) return rc;
+        CU(cudaMemsetAsync(b->counters.p + 2, 0, sizeof(uint32_t), st));
+        // tuning hits go to the survivors' buffer (its count is reset), then are dropped
+        const uint64_t lim = std::max<uint64_t>(16, (uint64_t)nseg * 4096 / (uint64_t)w);
+        if ((rc = launch_wave(e, dq, nq_all, u, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n)))
+          return rc;
+        CU(cudaEventRecord(e->ev[0], st));
+        CU(cudaMemsetAsync(b->tot.p + 3, 0, sizeof(uint64_t), st));
+        auto fn = u == 16 ? k_bwalk<16> : k_bwalk<8>;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
+        fn<<<std::max(per_sm, 1) * e->num_sms, BW_THREADS, 0, st>>>(
+            b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->chunk_seg.p, b->P.p,
+            b->Pinv.p, b->tot.p, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
+        CU(cudaGetLastError());
+        e->launches++;
+        CU(cudaEventRecord(e->ev[1], st));
+        CU(cudaEventSynchronize(e->ev[1]));
+        float ms = 0;
+        CU(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
+        // steps timed: the chunks walked (the wave may hold fewer than lim), each
+        // with the chunk size of the wave's first job, whose primes come first
+        uint64_t nch = 0;
+        CU(cudaMemcpy(&nch, b->tot.p + 2, sizeof nch, cudaMemcpyDeviceToHost));
+        const BJob& J0 = b->hjobs[T->batch[0].job];
+        const double steps = (double)std::min<uint64_t>(lim, nch) * J0.chunk * std::max<uint32_t>(J0.nsteps, 1);
+        const float per_step = (float)(ms / std::max(steps, 1.0));
+        if (per_step < best) {
+          best = per_step;
+          b->tuned_work = w;
+          b->tuned_unroll = u;
         }
-      if ((rc = upload_jobs(b->tuned_work))) return rc;
-      // the tuning waves added to the per-job prime counts: clear them
-      CU(cudaMemsetAsync(b->job_primes.p, 0, njobs * sizeof(unsigned long long), e->st));
-      CU(cudaMemsetAsync(b->job_sum.p, 0, njobs * sizeof(unsigned long long), e->st));
-      e->launches += 6;
-      tuned = true;
-    }
-    // the wave itself: a captured graph of the fixed sequence, replayed
-    if (!b->graph || b->graph_unroll != b->tuned_unroll ||
-        b->graph_q != dq || b->graph_nq != bt.nq) {
+      }
+    if ((rc = restore())) return rc;
+  }
+  if ((rc = set_chunks(e, smin, smax, b->tuned_work))) return rc;
+
+  // the wave itself: a captured graph of the fixed sequence, replayed
+  CU(cudaMemsetAsync(b->counters.p, 0, 2 * sizeof(uint32_t), st));
+  uint32_t raw = 0;
+  for (;;) {
+    if (!b->graph || b->graph_unroll != b->tuned_unroll || b->graph_q != dq || b->graph_nq != nq_all) {
       if (b->graph) cudaGraphExecDestroy(b->graph);
       b->graph = nullptr;
       cudaGraph_t g;
-      CU(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+      CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       const uint64_t launches0 = e->launches;
-      rc = launch_wave(e, dq, bt.nq, b->tuned_unroll, 0, b->hits.p, b->counters.p,
-                       (uint32_t)b->hits.n);
-      cudaError_t ce = cudaStreamEndCapture(e->st, &g);
+      rc = launch_wave(e, dq, nq_all, b->tuned_unroll, 0, b->hits.p, b->counters.p, (uint32_t)b->hits.n);
+      cudaError_t ce = cudaStreamEndCapture(st, &g);
       e->launches = launches0;
       if (rc) return rc;
       if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
@@ -880,46 +959,118 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
       if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
       b->graph_unroll = b->tuned_unroll;
       b->graph_q = dq;
-      b->graph_nq = bt.nq;
+      b->graph_nq = nq_all;
     }
-    CU(cudaGraphLaunch(b->graph, e->st));
+    CU(cudaGraphLaunch(b->graph, st));
     e->launches += 9;
-    ++waves;
-  }
-
-  // output rule, then group by job
-  CU(cudaEventRecord(e->ev[4], e->st));
-  CU(cudaMemcpyAsync(e->h_pinned, b->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
-  CU(cudaStreamSynchronize(e->st));
-  const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
-  if (raw > b->hits.n) {
-    // more candidates than the buffer: grow it and run the whole batch again
+    CU(cudaMemcpyAsync(e->h_pinned, b->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    raw = ((uint32_t*)e->h_pinned)[0];
+    if (raw <= b->hits.n) break;
+    // more candidates than the buffer: grow it (a new graph), put the slot
+    // counters back and walk the wave again
     if ((rc = b->hits.ensure((size_t)raw * 2))) return rc;
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
-    return pps_run_batch(e, jobs, njobs, out, cap, nout, job_offsets, bst);
+    if ((rc = restore())) return rc;
+    CU(cudaMemsetAsync(b->counters.p, 0, 2 * sizeof(uint32_t), st));
   }
+  if (raw_hits) *raw_hits += raw;
+
+  // output rule per candidate, with its job's parameters
   if (raw) {
-    uint32_t blocks = (raw * 32u + 255u) / 256u;
-    if (blocks > 4096u) blocks = 4096u;
-    k_bfilter<<<blocks, 256, 0, e->st>>>(b->hits.p, b->counters.p, (uint32_t)b->hits.n, b->jobs.p, e->small_q.p,
-                                         e->nsmall, b->out.p, b->counters.p + 1, (uint32_t)b->out.n);
-    CU(cudaGetLastError());
-    e->launches++;
+    CU(cudaEventRecord(e->ev[4], st));
+    uint32_t nf = 0;
+    for (;;) {
+      CU(cudaMemsetAsync(b->counters.p + 1, 0, sizeof(uint32_t), st));
+      uint32_t blocks = (raw * 32u + 255u) / 256u;
+      if (blocks > 4096u) blocks = 4096u;
+      k_bfilter<<<blocks, 256, 0, st>>>(b->hits.p, b->counters.p, (uint32_t)b->hits.n, b->jobs.p, e->small_q.p,
+                                        e->nsmall, b->out.p, b->counters.p + 1, (uint32_t)b->out.n);
+      CU(cudaGetLastError());
+      e->launches++;
+      CU(cudaMemcpyAsync(e->h_pinned, b->counters.p + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      CU(cudaStreamSynchronize(st));
+      nf = ((uint32_t*)e->h_pinned)[0];
+      if (nf <= b->out.n) break;
+      if ((rc = b->out.ensure((size_t)nf * 2))) return rc;  // the filter is re-run into the larger buffer
+    }
+    CU(cudaEventRecord(e->ev[5], st));
+    if (nf && survivors) {
+      const size_t at = survivors->size();
+      survivors->resize(at + nf);
+      CU(cudaMemcpyAsync(survivors->data() + at, b->out.p, nf * sizeof(pps_hit), cudaMemcpyDeviceToHost, st));
+      CU(cudaStreamSynchronize(st));
+      std::sort(survivors->begin() + at, survivors->end(), [](const pps_hit& x, const pps_hit& y) {
+        if (x.idx != y.idx) return x.idx < y.idx;
+        if (x.p != y.p) return x.p < y.p;
+        if (x.k != y.k) return x.k < y.k;
+        return x.n < y.n;
+      });
+    }
+    CU(cudaEventSynchronize(e->ev[5]));
+    float fms = 0;
+    CU(cudaEventElapsedTime(&fms, e->ev[4], e->ev[5]));
+    if (filter_ms) *filter_ms += fms;
   }
-  CU(cudaEventRecord(e->ev[5], e->st));
-  CU(cudaMemcpyAsync(e->h_pinned, b->counters.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
-  CU(cudaStreamSynchronize(e->st));
-  const uint32_t nf = ((uint32_t*)e->h_pinned)[1];
-  if (nf > b->out.n) return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "%u factors exceed the batch buffer", nf);
-  std::vector<pps_hit> surv(nf);
-  if (nf) CU(cudaMemcpy(surv.data(), b->out.p, nf * sizeof(pps_hit), cudaMemcpyDeviceToHost));
+  return PPS_OK;
+}
+
+extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t njobs, pps_factor* out,
+                             size_t cap, size_t* nout, size_t* job_offsets, pps_batch_stats* bst) {
+  if (!e || (!jobs && njobs)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  if (njobs > MAX_JOBS) return set_err(PPS_ERR_INVALID_PARAM, "at most %u jobs per batch", MAX_JOBS);
+  for (size_t j = 0; j < njobs; ++j)
+    if (jobs[j].step < 1 || jobs[j].step > 32 || jobs[j].pmin <= (1ull << 32))
+      return set_err(PPS_ERR_INVALID_PARAM, "job %zu not normalized", j);
+  int rc;
+  if ((rc = batch_prepare(e))) return rc;
+  BatchState* b = e->batch;
+  if (bst) memset(bst, 0, sizeof *bst);
+  CU(cudaEventRecord(e->ev[6], e->st));
+
+  // jobs j in slots j; pieces of at most one batch, most expensive jobs first
+  // (steps per prime x range width), packed into waves in that order
+  if ((rc = batch_set_jobs(e, 0, jobs, njobs))) return rc;
+  std::vector<size_t> order(njobs);
+  for (size_t j = 0; j < njobs; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    const double cx = (double)b->hjobs[x].nsteps * (double)(jobs[x].pmax - jobs[x].pmin);
+    const double cy = (double)b->hjobs[y].nsteps * (double)(jobs[y].pmax - jobs[y].pmin);
+    return cx > cy;
+  });
+  std::vector<BatchPiece> pieces;
+  const uint64_t span = batch_max_piece_span();
+  for (size_t j : order)
+    for (uint64_t lo = jobs[j].pmin | 1ull; lo < jobs[j].pmax; lo += span)
+      pieces.push_back(BatchPiece{lo, std::min(jobs[j].pmax, lo + span), (uint32_t)j});
+  std::vector<pps_hit> surv;
+  uint64_t raw = 0;
+  double fms = 0;
+  int waves = 0;
+  for (size_t a = 0; a < pieces.size();) {
+    uint64_t segs = 0;
+    size_t z = a;
+    while (z < pieces.size() && z - a < WAVE_BATCHES) {
+      const uint64_t ns = batch_piece_segments(pieces[z].lo, pieces[z].hi);
+      if (segs + ns > WAVE_SEGS) break;
+      segs += ns;
+      ++z;
+    }
+    if ((rc = batch_wave(e, pieces.data() + a, z - a, &surv, &raw, &fms))) return rc;
+    ++waves;
+    a = z;
+  }
+  CU(cudaEventRecord(e->ev[7], e->st));
+  CU(cudaEventSynchronize(e->ev[7]));
+  // survivors by job, each job's in (p, k, n) order
   std::sort(surv.begin(), surv.end(), [](const pps_hit& x, const pps_hit& y) {
     if (x.idx != y.idx) return x.idx < y.idx;
     if (x.p != y.p) return x.p < y.p;
     if (x.k != y.k) return x.k < y.k;
     return x.n < y.n;
   });
+  const size_t nf = surv.size();
   if (nout) *nout = nf;
   if (job_offsets) {
     size_t k = 0;
@@ -937,36 +1088,29 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     }
   }
   if (bst) {
-    std::vector<unsigned long long> jp(njobs), js(njobs);
-    if (njobs) {
-      CU(cudaMemcpy(jp.data(), b->job_primes.p, njobs * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-      CU(cudaMemcpy(js.data(), b->job_sum.p, njobs * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    }
+    std::vector<uint64_t> jp(njobs), js(njobs);
+    if (njobs && (rc = batch_job_counts(e, 0, njobs, jp.data(), js.data()))) return rc;
     for (size_t j = 0; j < njobs; ++j) {
       bst->primes += jp[j];
       bst->prime_sum += js[j];
-      bst->steps += jp[j] * hj[j].nsteps;
+      bst->steps += jp[j] * b->hjobs[j].nsteps;
     }
     bst->raw_hits = raw;
     bst->factors = nf;
     bst->waves = (uint32_t)waves;
     bst->chunk = (uint32_t)b->tuned_work;
     bst->unroll = (uint32_t)b->tuned_unroll;
-    float ms = 0, fms = 0;
-    CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[5]));
-    CU(cudaEventElapsedTime(&fms, e->ev[4], e->ev[5]));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
     bst->total_ms = ms;
     bst->filter_ms = fms;
   }
-  if (out && nf > cap) return set_err(PPS_ERR_OVERFLOW, "%u factors, buffer holds %zu", nf, cap);
+  if (out && nf > cap) return set_err(PPS_ERR_OVERFLOW, "%zu factors, buffer holds %zu", nf, cap);
   return PPS_OK;
 }
 
 extern "C" int pps_batch_job_primes(pps_engine* e, size_t njobs, uint64_t* primes, uint64_t* sums) {
   if (!e || !e->batch || !e->batch->ready) return set_err(PPS_ERR_INVALID_PARAM, "no batch has run");
-  if (njobs > e->batch->job_primes.n) return set_err(PPS_ERR_INVALID_PARAM, "njobs too large");
-  CU(cudaSetDevice(e->device));
-  if (primes) CU(cudaMemcpy(primes, e->batch->job_primes.p, njobs * 8, cudaMemcpyDeviceToHost));
-  if (sums) CU(cudaMemcpy(sums, e->batch->job_sum.p, njobs * 8, cudaMemcpyDeviceToHost));
-  return PPS_OK;
+  if (njobs > MAX_JOBS) return set_err(PPS_ERR_INVALID_PARAM, "njobs too large");
+  return batch_job_counts(e, 0, njobs, primes, sums);
 }

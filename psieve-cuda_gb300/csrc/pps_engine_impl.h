@@ -91,3 +91,23 @@ uint32_t isqrt64(uint64_t x);
 int prepare_sieving_primes(pps_engine* e, uint32_t qmax, uint64_t pmax, const uint32_t** dq,
                            BaseTable* bt);
 void batch_state_free(pps_engine* e);
+
+// ---- wave-level interface of the batched form (pps_batch.cu), shared by
+// pps_run_batch and the serving loop (pps_server.cu).  Jobs live in device
+// slots; a wave walks pieces (p sub-ranges of slotted jobs) and returns the
+// survivors of the output rule, sorted by (slot, p, k, n).
+struct BatchPiece {
+  uint64_t lo, hi;  // p in [lo, hi)
+  uint32_t slot;
+};
+uint32_t batch_max_slots();
+uint64_t batch_wave_segments();          // segments one wave holds
+uint64_t batch_piece_segments(uint64_t lo, uint64_t hi);
+uint64_t batch_max_piece_span();         // widest p range of one piece
+int batch_prepare(pps_engine* e);
+// normalised jobs into slots [slot0, slot0 + n); their prime counters start at zero
+int batch_set_jobs(pps_engine* e, uint32_t slot0, const pps_job_params* jobs, size_t n);
+int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pps_hit>* survivors,
+               uint64_t* raw_hits, double* filter_ms);
+int batch_job_counts(pps_engine* e, uint32_t slot0, size_t n, uint64_t* primes, uint64_t* sums);
+void batch_tuning(pps_engine* e, uint32_t* work, uint32_t* unroll);

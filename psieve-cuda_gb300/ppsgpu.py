@@ -81,6 +81,37 @@ class BatchStats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("factor_bytes", ctypes.c_uint64), ("max_jobs", ctypes.c_uint32),
+                ("wave_segments", ctypes.c_uint32)]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [("primes", ctypes.c_uint64), ("prime_sum", ctypes.c_uint64),
+                ("factors", ctypes.c_uint64), ("latency_ms", ctypes.c_double),
+                ("status", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64),
+                ("completed", ctypes.c_uint64), ("refused", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("queued", ctypes.c_uint64),
+                ("running", ctypes.c_uint64), ("reserved_bytes", ctypes.c_uint64),
+                ("primes", ctypes.c_uint64), ("steps", ctypes.c_uint64),
+                ("waves", ctypes.c_uint64), ("chunk", ctypes.c_uint32),
+                ("unroll", ctypes.c_uint32), ("busy_ms", ctypes.c_double),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+PPS_JOB_QUEUED, PPS_JOB_RUNNING, PPS_JOB_DONE, PPS_JOB_FAILED = 0, 1, 2, 3
+
+
 class PPSError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"ppsgpu error {code}: {msg}")
@@ -131,6 +162,13 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
                                          ctypes.c_void_p, ctypes.c_size_t, szp, szp,
                                          P(BatchStats)]),
         "pps_batch_job_primes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, u64p, u64p]),
+        "pps_server_create": (ctypes.c_int, [ctypes.c_int, P(ServerConfig), P(ctypes.c_void_p)]),
+        "pps_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+        "pps_job_submit": (ctypes.c_int, [ctypes.c_void_p, P(JobParams), u64p]),
+        "pps_job_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, P(ctypes.c_int)]),
+        "pps_job_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double,
+                                        ctypes.c_void_p, ctypes.c_size_t, szp, P(JobResult)]),
+        "pps_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(ServerStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -341,3 +379,60 @@ def mixed_jobs(seed: int = 1, count: int = 512, scale_p: float = 1.0, scale_n: f
         jobs.append(jp)
         meta.append((spec, repairs))
     return jobs, meta
+
+
+class Server:
+    """The serving loop (pps_server_*): submit normalised jobs, wait for each
+    job's sorted factor list."""
+
+    def __init__(self, device: int = 0, factor_bytes: int = 0, max_jobs: int = 0,
+                 wave_segments: int = 0, lib=None):
+        self.lib = lib or load()
+        cfg = ServerConfig(factor_bytes, max_jobs, wave_segments)
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.pps_server_create(device, ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.pps_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, jp: JobParams) -> int:
+        jid = ctypes.c_uint64()
+        _check(self.lib, self.lib.pps_job_submit(self.h, ctypes.byref(jp), ctypes.byref(jid)))
+        return jid.value
+
+    def poll(self, jid: int) -> int:
+        st = ctypes.c_int()
+        _check(self.lib, self.lib.pps_job_poll(self.h, jid, ctypes.byref(st)))
+        return st.value
+
+    def wait(self, jid: int, timeout: float = -1.0) -> tuple[np.ndarray, JobResult]:
+        """Block until job `jid` is done (or `timeout` seconds); returns its
+        factors (FACTOR_DTYPE, sorted by p, k, n) and its JobResult."""
+        n = ctypes.c_size_t()
+        res = JobResult()
+        _check(self.lib, self.lib.pps_job_wait(self.h, jid, timeout, None, 0, ctypes.byref(n),
+                                               ctypes.byref(res)))
+        out = np.zeros(max(n.value, 1), dtype=FACTOR_DTYPE)
+        _check(self.lib, self.lib.pps_job_wait(self.h, jid, 0.0, out.ctypes.data_as(ctypes.c_void_p),
+                                               out.size, ctypes.byref(n), ctypes.byref(res)))
+        return out[: n.value], res
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(self.lib, self.lib.pps_server_get_stats(self.h, ctypes.byref(st)))
+        return st

@@ -1,0 +1,84 @@
+"""The serving loop (pps_server_*, continuous batching) on the GPU: each job's
+factor list and prime fingerprint from the server, in a mix of concurrent jobs,
+must be exactly what the one-job path (and the reference) gives for that job
+alone; admission limits and refusals behave as documented."""
+from __future__ import annotations
+
+import pytest
+
+from helpers import args_to_spec, lines_of
+
+pytestmark = pytest.mark.gpu
+
+
+def test_server_mix_equals_jobs_alone(pps, engine):
+    jobs, meta = pps.mixed_jobs(seed=11, count=40, scale_p=2e-3, scale_n=2e-2)
+    with pps.Server(0) as srv:
+        ids = [srv.submit(jp) for jp in jobs]
+        results = [srv.wait(i) for i in ids]
+        st = srv.stats()
+    for (fac, res), jp, m in zip(results, jobs, meta):
+        want, wst = engine.run_job(jp)
+        assert pps.factors_to_tuples(fac) == pps.factors_to_tuples(want), m
+        assert res.primes == wst.primes and res.prime_sum == wst.prime_sum, m
+        assert res.status == 0 and res.latency_ms > 0
+    assert st.completed == len(jobs) and st.failed == 0 and st.refused == 0
+    assert st.queued == 0 and st.running == 0 and st.reserved_bytes == 0
+    assert st.waves >= 1 and 0 < st.p50_ms <= st.p99_ms
+
+
+def test_server_reference_cases(pps, ref_cases):
+    names = sorted(k for k in ref_cases if k.startswith("rand"))[:12]
+    with pps.Server(0, wave_segments=64) as srv:  # small waves: jobs span several
+        ids = {n: srv.submit(pps.normalize(**args_to_spec(ref_cases[n]["args"]))) for n in names}
+        for n in names:
+            fac, res = srv.wait(ids[n])
+            assert lines_of(pps.factors_to_tuples(fac)) == sorted(set(ref_cases[n]["lines"])), n
+            assert res.primes == ref_cases[n]["count"], n
+
+
+def test_server_admission_limits(pps, engine):
+    jobs, _ = pps.mixed_jobs(seed=5, count=9, scale_p=1e-3, scale_n=1e-2)
+    # two slots: the other jobs wait in the queue and are admitted as slots free
+    with pps.Server(0, max_jobs=2) as srv:
+        ids = [srv.submit(jp) for jp in jobs]
+        got = [srv.wait(i) for i in ids]
+        st = srv.stats()
+    assert st.admitted == len(jobs) and st.completed == len(jobs)
+    for (fac, _), jp in zip(got, jobs):
+        want, _ = engine.run_job(jp)
+        assert pps.factors_to_tuples(fac) == pps.factors_to_tuples(want)
+
+
+def test_server_refusal_under_small_budget(pps):
+    small = pps.normalize(pmin=10**12, pmax=10**12 + 10**6, kmin=1201, kmax=1301, nmin=2000, nmax=2100)
+    # about 1.8e5 expected raw candidates: an 11.6 MB reservation against a 1 MiB budget
+    big = pps.normalize(pmin=10**12, pmax=10**12 + 10**9, kmin=3, kmax=9999, nmin=1000,
+                        nmax=1000000)
+    with pps.Server(0, factor_bytes=1 << 20) as srv:
+        with pytest.raises(pps.PPSError) as ei:
+            srv.submit(big)
+        assert ei.value.code == pps.PPS_ERR_INSUFFICIENT_RESOURCE
+        jid = srv.submit(small)
+        fac, res = srv.wait(jid)
+        st = srv.stats()
+    assert res.status == 0 and st.refused == 1 and st.completed == 1
+
+
+def test_server_wait_timeout_poll_and_unknown(pps):
+    jp = pps.normalize(pmin=42 * 10**12, pmax=42 * 10**12 + 2 * 10**9, kmin=1201, kmax=9999,
+                       nmin=2000000, nmax=3000000)
+    with pps.Server(0) as srv:
+        jid = srv.submit(jp)
+        with pytest.raises(pps.PPSError) as ei:
+            srv.wait(jid, timeout=0.0)
+        assert ei.value.code == pps.PPS_ERR_TIMEOUT
+        assert srv.poll(jid) in (pps.PPS_JOB_QUEUED, pps.PPS_JOB_RUNNING)
+        fac, res = srv.wait(jid)
+        assert res.status == 0 and res.primes > 0
+        with pytest.raises(pps.PPSError) as ei:
+            srv.poll(jid)  # released by the wait that returned its result
+        assert ei.value.code == pps.PPS_ERR_NOT_FOUND
+        with pytest.raises(pps.PPSError) as ei:
+            srv.submit(pps.JobParams())  # not normalised
+        assert ei.value.code == pps.PPS_ERR_INVALID_PARAM
