@@ -191,6 +191,59 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
             "batched_n_steps_per_s": bst.steps / t_batch}
 
 
+def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -> dict:
+    """Configuration 5: Poisson arrivals at each rate for `window` seconds of
+    jobs from the configuration-4 distribution, submitted to the serving loop
+    (pps_server_*); every submitted job is waited for.  Reports per rate the
+    aggregate primes/s (submission of the first job to the last result) and the
+    p50/p99 latency (submission to result ready) of the jobs."""
+    import numpy as np
+
+    import ppsgpu
+
+    need = int(max(rates) * window * 1.3) + 64
+    pool, _ = ppsgpu.mixed_jobs(seed=seed, count=need)
+    rng = np.random.default_rng(seed)
+    per_rate = []
+    with ppsgpu.Server(0) as srv:
+        for jp in pool[:8]:  # warm-up: walk tuning, graph capture, sieving primes
+            srv.wait(srv.submit(jp))
+        nxt = 8
+        for rate in rates:
+            ids = []
+            t0 = time.perf_counter()
+            t = 0.0
+            while True:
+                t += float(rng.exponential(1.0 / rate))
+                if t > window:
+                    break
+                delay = t0 + t - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append(srv.submit(pool[nxt % len(pool)]))
+                nxt += 1
+            lat, primes, factors = [], 0, 0
+            for jid in ids:
+                fac, res = srv.wait(jid)
+                lat.append(res.latency_ms)
+                primes += res.primes
+                factors += len(fac)
+            elapsed = time.perf_counter() - t0
+            lat_sorted = sorted(lat)
+
+            def rank(q):
+                return lat_sorted[max(1, int(np.ceil(q * len(lat_sorted)))) - 1] if lat_sorted else None
+
+            per_rate.append({"rate_jobs_per_s": rate, "jobs": len(ids), "seconds": elapsed,
+                             "primes_per_s": primes / elapsed, "factors": factors,
+                             "p50_ms": rank(0.50), "p99_ms": rank(0.99)})
+        st = srv.stats()
+    return {"workload": f"Poisson arrivals, {window:g} s per rate, jobs of the configuration-4 "
+                        f"distribution (seed {seed})",
+            "rates": per_rate, "waves": int(st.waves), "busy_ms": st.busy_ms,
+            "completed": int(st.completed), "failed": int(st.failed)}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = _dist()
     if rank != 0:
@@ -344,6 +397,7 @@ def run_gpu(args) -> None:
                           "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
     cpu = None if args.no_cpu else cpu_sample(args.ref_seconds)
     batched = None if args.no_batched else run_mixed(eng, args.mixed_jobs)
+    serving = None if args.no_serving else run_serving(window=args.serve_window)
     line = {"metric": METRIC, "value": value, "unit": "primes/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -357,7 +411,7 @@ def run_gpu(args) -> None:
                          "filter": sum(s.filter_ms for s in stats)},
             "factors": sum(s.factors for s in stats),
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "batched": batched}
+            "batched": batched, "serving": serving}
     print(json.dumps(line), flush=True)
     eng.close()
     if ws > 1:
@@ -415,6 +469,8 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-window", type=float, default=4.0)
     ap.add_argument("--mixed-jobs", type=int, default=512)
     ap.add_argument("--profile", type=int, nargs=2, metavar=("SPAN", "NWIDTH"))
     ap.add_argument("--profile-reps", type=int, default=1)

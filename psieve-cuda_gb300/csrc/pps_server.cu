@@ -81,7 +81,6 @@ struct pps_server {
   std::vector<uint32_t> free_slots;
   uint64_t reserved = 0;
   uint64_t next_id = 1;
-  int fatal = PPS_OK;  // a failure of the worker itself (jobs fail with it)
   pps_server_stats st{};
   std::vector<double> latencies;
 };
@@ -123,7 +122,8 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
   // the wave: one piece per job first (oldest first), then fill oldest first
   pieces.clear();
   const uint64_t cap = s->cfg.wave_segments;
-  const uint64_t span = batch_max_piece_span();
+  // a piece is at most one batch, and never more than the wave holds
+  const uint64_t span = std::min<uint64_t>(batch_max_piece_span(), cap * 2ull * pps::SEG_BITS);
   uint64_t segs = 0;
   std::vector<JobRec*> in_wave, finishing;
   auto take = [&](JobRec* j) -> bool {
@@ -227,8 +227,6 @@ extern "C" int pps_server_create(int device, const pps_server_config* cfg, pps_s
     return set_err(PPS_ERR_INVALID_PARAM, "max_jobs above %u", batch_max_slots());
   if (!c.wave_segments || c.wave_segments > batch_wave_segments())
     c.wave_segments = (uint32_t)batch_wave_segments();
-  if (c.wave_segments < batch_piece_segments(1ull << 33, (1ull << 33) + batch_max_piece_span()))
-    return set_err(PPS_ERR_INVALID_PARAM, "wave_segments below one piece");
   pps_engine* e = nullptr;
   int rc = pps_engine_create(device, &e);
   if (rc) return rc;
@@ -327,7 +325,7 @@ extern "C" int pps_job_wait(pps_server* s, uint64_t id, double timeout_s, pps_fa
     res->latency_ms = ms_between(j->t_submit, j->t_done);
     res->status = j->status;
   }
-  if (!out && nf) return PPS_OK;  // size query: the job stays for a later call
+  if (!out) return PPS_OK;  // size query: the job stays for a later call
   if (nf > cap) return set_err(PPS_ERR_OVERFLOW, "%zu factors, buffer holds %zu", nf, cap);
   if (nf) memcpy(out, j->factors.data(), nf * sizeof(pps_factor));
   const int status = j->status;
