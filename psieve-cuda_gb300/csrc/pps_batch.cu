@@ -76,8 +76,9 @@ struct BatchState {
   DevBuf<BJob> jobs;
   DevBuf<uint32_t> bitmap;      // WAVE_SEGS * SEG_WORDS
   DevBuf<uint32_t> seg_count, seg_off, chunk_count, chunk_off, chunk_seg;
+  DevBuf<uint32_t> large_items, large_off;  // per batch: large-prime work items, their prefix sums
   DevBuf<uint64_t> P, Pinv;
-  DevBuf<uint64_t> tot;         // [0] primes, [1] sum, [2] chunks, [3] work counter
+  DevBuf<uint64_t> tot;         // [0] primes, [1] sum, [2] chunks, [3] work counter, [4] large items
   DevBuf<unsigned long long> job_primes, job_sum;
   DevBuf<pps_hit> hits, out;
   DevBuf<uint32_t> counters;    // [0] raw, [1] survivors, [2] tuning hits, [3] large-sieve items
@@ -110,6 +111,8 @@ void batch_state_free(pps_engine* e) {
   b->chunk_count.release();
   b->chunk_off.release();
   b->chunk_seg.release();
+  b->large_items.release();
+  b->large_off.release();
   b->P.release();
   b->Pinv.release();
   b->tot.release();
@@ -129,10 +132,17 @@ namespace pps {
 
 __device__ __forceinline__ const WaveTables* wt(const uint8_t* t) { return (const WaveTables*)t; }
 
-// per batch: how many of the ascending sieving primes are <= its limit
-__global__ void k_bcounts(uint8_t* tables, const uint32_t* q, uint32_t nq_all) {
+constexpr uint32_t LARGE_Q_PER_ITEM = 8192;  // large sieving primes per work item
+
+// per batch: how many of the ascending sieving primes are <= its limit, and
+// its number of large-prime work items (0 past the last batch)
+__global__ void k_bcounts(uint8_t* tables, const uint32_t* q, uint32_t nq_all, uint32_t* large_items) {
   WaveTables* T = (WaveTables*)tables;
-  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < T->nbatch; b += gridDim.x * blockDim.x) {
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < WAVE_BATCHES; b += gridDim.x * blockDim.x) {
+    if (b >= T->nbatch) {
+      large_items[b] = 0;
+      continue;
+    }
     BBatch& B = T->batch[b];
     uint32_t lo = 0, hi = nq_all;
     while (lo < hi) {
@@ -158,6 +168,7 @@ __global__ void k_bcounts(uint8_t* tables, const uint32_t* q, uint32_t nq_all) {
     }
     B.nq_tiny = t;
     B.nq_seg = s;
+    large_items[b] = (lo - s + LARGE_Q_PER_ITEM - 1) / LARGE_Q_PER_ITEM;
   }
 }
 
@@ -187,28 +198,49 @@ __device__ __forceinline__ uint64_t b_mod(uint64_t x, uint64_t q, uint64_t m) {
   return r;
 }
 
-constexpr uint32_t LARGE_SLICES = 64;  // work items per batch in the large-prime pass
-
-// Large sieving primes (q >= SEG_BITS) into the wave bitmap.  Work items are
-// (batch, slice) pairs taken from a device counter, so a wave of a few wide
-// batches and one of many narrow batches both fill the GPU.
+// Large sieving primes (q >= SEG_BITS) into the wave bitmap.  Work items of
+// LARGE_Q_PER_ITEM primes each are numbered batch by batch (item_off = prefix
+// sums of the per-batch item counts) and taken in order from a device counter,
+// so the GPU works on one or two batches at a time: their bitmap (at most
+// 128 MB) stays in L2 while its bits are cleared.  A block's items only ever
+// increase, so it finds each item's batch by galloping forward from the last one.
 __global__ void k_bsieve_large(const uint8_t* tables, const uint32_t* q, const uint64_t* qm, uint32_t* bitmap,
-                               uint32_t* item_counter) {
-  __shared__ uint32_t s_item;
+                               const uint32_t* item_off, const uint64_t* item_total, uint32_t* item_counter) {
+  __shared__ uint32_t s_item, s_batch;
   const WaveTables* T = wt(tables);
-  const uint32_t nitems = T->nbatch * LARGE_SLICES;
+  const uint32_t nitems = (uint32_t)*item_total, nb = T->nbatch;
+  uint32_t cur = 0;  // thread 0: batch of the block's last item
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(item_counter, 1u);
+    if (threadIdx.x == 0) {
+      const uint32_t item = atomicAdd(item_counter, 1u);
+      if (item < nitems) {
+        // last batch b >= cur with item_off[b] <= item
+        uint32_t step = 1, lo = cur, hi = cur + 1;
+        while (hi < nb && item_off[hi] <= item) {
+          lo = hi;
+          hi = lo + step;
+          step <<= 1;
+        }
+        if (hi > nb) hi = nb;
+        while (hi - lo > 1) {
+          const uint32_t mid = lo + (hi - lo) / 2;
+          if (item_off[mid] <= item) lo = mid; else hi = mid;
+        }
+        cur = lo;
+      }
+      s_item = item;
+      s_batch = cur;
+    }
     __syncthreads();
-    const uint32_t item = s_item;
+    const uint32_t item = s_item, bidx = s_batch;
     __syncthreads();
     if (item >= nitems) return;
-    const BBatch B = T->batch[item / LARGE_SLICES];
-    const uint32_t slice = item % LARGE_SLICES;
-    if (B.nq <= B.nq_seg) continue;
+    const BBatch B = T->batch[bidx];
     uint32_t* bm = bitmap + (size_t)B.seg0 * SEG_WORDS;
     const uint64_t hi = B.lo + 2ull * B.nbits;
-    for (uint32_t i = B.nq_seg + slice * blockDim.x + threadIdx.x; i < B.nq; i += LARGE_SLICES * blockDim.x) {
+    const uint32_t i0 = B.nq_seg + (item - item_off[bidx]) * LARGE_Q_PER_ITEM;
+    const uint32_t i1 = min(B.nq, i0 + LARGE_Q_PER_ITEM);
+    for (uint32_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const uint64_t qq = q[i];
       if (qq * qq >= hi) continue;
       uint64_t st = qq * qq;
@@ -613,14 +645,15 @@ int ensure_state(pps_engine* e) {
       return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "pinned table staging");
     if ((rc = b->bitmap.ensure((size_t)WAVE_SEGS * SEG_WORDS))) return rc;
     if ((rc = b->seg_count.ensure(WAVE_SEGS)) || (rc = b->seg_off.ensure(WAVE_SEGS)) ||
-        (rc = b->chunk_count.ensure(WAVE_SEGS)) || (rc = b->chunk_off.ensure(WAVE_SEGS)))
+        (rc = b->chunk_count.ensure(WAVE_SEGS)) || (rc = b->chunk_off.ensure(WAVE_SEGS)) ||
+        (rc = b->large_items.ensure(WAVE_BATCHES)) || (rc = b->large_off.ensure(WAVE_BATCHES)))
       return rc;
     // p > 2^32: odd primes are fewer than 1/10 of the odd candidates
     b->prime_cap = (uint64_t)WAVE_SEGS * SEG_BITS / 10 + 4096;
     if ((rc = b->P.ensure(b->prime_cap)) || (rc = b->Pinv.ensure(b->prime_cap))) return rc;
     // at most prime_cap/32 + one partial chunk per segment (smallest chunk: 32)
     if ((rc = b->chunk_seg.ensure(b->prime_cap / 32 + WAVE_SEGS))) return rc;
-    if ((rc = b->tot.ensure(4))) return rc;
+    if ((rc = b->tot.ensure(8))) return rc;
     if ((rc = b->counters.ensure(4))) return rc;
     if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
     if (cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming) != cudaSuccess)
@@ -639,16 +672,20 @@ int ensure_state(pps_engine* e) {
   return PPS_OK;
 }
 
+constexpr uint64_t WAVE_KERNELS = 10;  // kernels in one wave's launch sequence
+
 // The fixed per-wave launch sequence (everything reads counts from the tables).
 int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, uint64_t chunk_limit,
                 pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
   BatchState* b = e->batch;
   cudaStream_t st = e->st;
   CU(cudaMemsetAsync(b->bitmap.p, 0xff, (size_t)WAVE_SEGS * SEG_WORDS * 4, st));
-  CU(cudaMemsetAsync(b->tot.p, 0, 4 * sizeof(uint64_t), st));
-  k_bcounts<<<(WAVE_BATCHES + 255) / 256, 256, 0, st>>>(b->tables.p, dq, nq_all);
+  CU(cudaMemsetAsync(b->tot.p, 0, 8 * sizeof(uint64_t), st));
+  k_bcounts<<<(WAVE_BATCHES + 255) / 256, 256, 0, st>>>(b->tables.p, dq, nq_all, b->large_items.p);
+  k_bscan<<<1, 1024, 0, st>>>(b->large_items.p, b->large_off.p, WAVE_BATCHES, b->tot.p + 4);
   CU(cudaMemsetAsync(b->counters.p + 3, 0, sizeof(uint32_t), st));
-  k_bsieve_large<<<e->num_sms * 8, 256, 0, st>>>(b->tables.p, dq, b->qm.p, b->bitmap.p, b->counters.p + 3);
+  k_bsieve_large<<<e->num_sms * 8, 256, 0, st>>>(b->tables.p, dq, b->qm.p, b->bitmap.p, b->large_off.p,
+                                                 b->tot.p + 4, b->counters.p + 3);
   k_bsieve_seg<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, dq, b->bitmap.p, b->seg_count.p);
   k_bscan<<<1, 1024, 0, st>>>(b->seg_count.p, b->seg_off.p, WAVE_SEGS, b->tot.p);
   k_bexpand<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, b->bitmap.p, b->seg_off.p, b->P.p, b->Pinv.p,
@@ -665,7 +702,7 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, 
                                   b->chunk_seg.p, b->P.p, b->Pinv.p, b->tot.p, chunk_limit, hits, hit_count,
                                   hit_cap);
   CU(cudaGetLastError());
-  e->launches += 9;  // the kernels above, each once
+  e->launches += WAVE_KERNELS;
   return PPS_OK;
 }
 
@@ -962,7 +999,7 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
       b->graph_nq = nq_all;
     }
     CU(cudaGraphLaunch(b->graph, st));
-    e->launches += 9;
+    e->launches += WAVE_KERNELS;
     CU(cudaMemcpyAsync(e->h_pinned, b->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     raw = ((uint32_t*)e->h_pinned)[0];
