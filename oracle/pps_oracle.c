@@ -83,9 +83,10 @@ int ppo_normalize(ppo_params *o, uint64_t pmin, uint64_t pmax, uint64_t kmin,
 {
   const uint64_t PMAX_MAX = (uint64_t)1 << 62; /* main.h:43 */
   memset(o, 0, sizeof *o);
-  if (kstep == 0) kstep = 2;      /* pps/app.c:57 KSTEP */
-  if (koffset == 0) koffset = 1;  /* pps/app.c:58 KOFFSET */
-  if (c != 1 && c != -1) return PPO_ERR_INVALID_PARAM;
+  if (c != 1 && c != -1 && c != PPO_TWIN) return PPO_ERR_INVALID_PARAM;
+  /* pps/app.c:53-58 KSTEP/KOFFSET: 6/3 in the SEARCH_TWIN build, else 2/1 */
+  if (kstep == 0) kstep = c == PPO_TWIN ? 6 : 2;
+  if (koffset == 0) koffset = c == PPO_TWIN ? 3 : 1;
 
   /* main.c:916-931 */
   if (pmin < 3) pmin = 3;
@@ -119,6 +120,9 @@ int ppo_normalize(ppo_params *o, uint64_t pmin, uint64_t pmax, uint64_t kmin,
   /* pps/appcu.cu:158-204 */
   if (nstep > nmax - nmin + 1) nstep = nmax - nmin + 1;
   if ((((uint64_t)1) << (64 - nstep)) > pmin) return PPO_ERR_INVALID_PARAM;
+  /* pps/appcu.cu:177-180: the twin walk steps one n less, so that consecutive
+     steps overlap by one n (its even value is tested for i <= nstep) */
+  if (c == PPO_TWIN) nstep--;
   if (nstep >= 32 && nstep < 48 && (((uint64_t)1) << 32) <= pmin) nstep = 32;
   if (lg2_u64(nmin) < 6) return PPO_ERR_INVALID_PARAM;
   /* pps/appcu.cu:236-239 */
@@ -198,9 +202,52 @@ static inline uint64_t shift_down(uint64_t k, uint64_t p, uint64_t ps, uint32_t 
   return r >= p ? r - p : r;
 }
 
+static void emit(ppo_factor *out, size_t cap, size_t *found, uint64_t p, uint64_t k, uint32_t n,
+                 int32_t c)
+{
+  if (*found < cap) {
+    out[*found].p = p; out[*found].k = k;
+    out[*found].n = n; out[*found].c = c;
+  }
+  (*found)++;
+}
+
+/* The SEARCH_TWIN build of test_one_p (pps/app.c:1071-1107): one walk of
+   k0 = 2^-n serves both sides, k0 itself for -1 and p - k0 for +1.  At nmin
+   the odd one of the two is tested as it is; then at every step the even one,
+   with i = ctz <= nstep, since the steps overlap by one n.  filter = 0 gives
+   the raw candidates (k in range, n < nmax) with their sides. */
+static size_t walk_twin(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t cap, int filter)
+{
+  size_t found = 0;
+  const uint64_t ps = neg_inv64(p);
+  uint64_t k0 = powmod64((p + 1) / 2, pp->nmin, p);
+  uint32_t n = pp->nmin;
+  const uint32_t s = pp->nstep;
+  uint64_t kpos = (k0 & 1) ? k0 : p - k0;
+  if (kpos <= pp->kmax && kpos >= pp->kmin) {
+    const int32_t c = kpos == k0 ? -1 : 1;
+    if (filter ? ppo_test_factor(pp, kpos, n, c) : n < pp->nmax) emit(out, cap, &found, p, kpos, n, c);
+  }
+  do {
+    kpos = (k0 & 1) ? p - k0 : k0;
+    const int i = __builtin_ctzll(kpos);
+    const uint64_t kk = kpos >> i;
+    if (kk <= pp->kmax && kk >= pp->kmin && (uint32_t)i <= s) {
+      const int32_t c = kpos == k0 ? -1 : 1;
+      const uint32_t ni = n + (uint32_t)i;
+      if (filter ? ppo_test_factor(pp, kk, ni, c) : ni < pp->nmax) emit(out, cap, &found, p, kk, ni, c);
+    }
+    n += s;
+    k0 = shift_down(k0, p, ps, s);
+  } while (n < pp->nmax);
+  return found;
+}
+
 /* pps/app.c:1037-1121 test_one_p over the whole [nmin, nmax). */
 size_t ppo_walk_prime(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t cap)
 {
+  if (pp->c == PPO_TWIN) return walk_twin(pp, p, out, cap, 1);
   size_t found = 0;
   const uint64_t ps = neg_inv64(p);
   /* 2^-nmin mod p (pps/app.c:1014-1035 invpowmod_REDClr computes the same). */
@@ -231,6 +278,7 @@ size_t ppo_walk_prime(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t 
    as ppo_walk_prime; c is set to the job's sign. */
 size_t ppo_walk_prime_raw(const ppo_params *pp, uint64_t p, ppo_factor *out, size_t cap)
 {
+  if (pp->c == PPO_TWIN) return walk_twin(pp, p, out, cap, 0);
   size_t found = 0;
   const uint64_t ps = neg_inv64(p);
   uint64_t k = powmod64((p + 1) / 2, pp->nmin, p);

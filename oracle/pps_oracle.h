@@ -34,11 +34,15 @@ extern "C" {
 #define PPO_ERR_INVALID_PARAM (-178)
 #define PPO_ERR_INSUFFICIENT_RESOURCE (-198)
 
+/* c of a twin job: both sides in one walk (the reference's SEARCH_TWIN build,
+   tpsieve); each reported factor carries its own c = +1 or -1. */
+#define PPO_TWIN 2
+
 typedef struct {
   uint64_t pmin, pmax;   /* primes p: pmin <= p < pmax */
   uint64_t kmin, kmax;   /* rounded to kstep*b+koffset */
   uint32_t nmin, nmax;   /* n in [nmin, nmax) */
-  int32_t  c;            /* +1 Proth (k*2^n+1), -1 Riesel (k*2^n-1) */
+  int32_t  c;            /* +1 Proth (k*2^n+1), -1 Riesel (k*2^n-1), PPO_TWIN both */
   uint32_t kstep, koffset;
   uint32_t qmax;         /* largest sieving prime bound actually used */
   uint32_t nstep;        /* n values covered per walk step */

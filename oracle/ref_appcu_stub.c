@@ -45,6 +45,9 @@ void cuda_init(void)
     bmsg("Error: pmin is not large enough (or nmax is close to nmin).\n");
     bexit(ERR_INVALID_PARAM);
   }
+#ifdef SEARCH_TWIN
+  ld_nstep--; /* pps/appcu.cu:177-180 */
+#endif
   if (ld_nstep >= 32 && ld_nstep < 48 && (((uint64_t)1) << 32) <= pmin)
     ld_nstep = 32;
   ld_bbits = stub_lg2(nmin);

@@ -215,6 +215,51 @@ def main() -> None:
             (HERE / dst).write_text("\n".join(lines) + "\n")
         cases = json.loads((HERE / "ref_cases.json").read_text())
         (HERE / "many_n_test_39.txt").write_text("\n".join(cases["many_n_test"]["lines"]) + "\n")
+    if "twin" in which:
+        # the reference's twin build (tpsieve_ref: -DSEARCH_TWIN, both sides per walk,
+        # k == 3 mod 6 unless -M/-s say otherwise)
+        rng = random.Random(99)
+        cases = [
+            ("twin_small", ["-p1e12", "-P1000050000000", "-k1201", "-K9999", "-n2000", "-N3000"]),
+            ("twin_all_odd_k", ["-p1e12", "-P1000020000000", "-k3", "-K9999", "-n2000", "-N3000",
+                                "-M2", "-s1"]),
+            ("twin_c2_slice", [f"-p{42 * 10**12}", f"-P{42 * 10**12 + 2 * 10**6}", "-k1201",
+                               "-K9999", "-n2000000", "-N3000000"]),
+            ("twin_nstep32", [f"-p{2**40}", f"-P{2**40 + 10**7}", "-k3", "-K999", "-n100000",
+                              "-N101000", "-M2", "-s1"]),
+            ("twin_wide_n", ["-p1e12", "-P1000020000000", "-k3", "-K9999", "-n1000", "-N100000",
+                             "-M2", "-s1"]),
+            ("twin_wide_n3", ["-p2e12", "-P2000030000000", "-k1201", "-K9999", "-n1000",
+                              "-N200000"]),
+        ]
+        for i in range(10):
+            pmin = int(10 ** rng.uniform(11.5, 15.5))
+            kmin = rng.randrange(3, 3000)
+            n0 = rng.randrange(200, 200000)
+            cases.append((f"twin_rand{i:02d}", [f"-p{pmin}", f"-P{pmin + rng.randrange(10**6, 10**7)}",
+                                                f"-k{kmin}", f"-K{kmin + rng.randrange(100, 9000)}",
+                                                f"-n{n0}", f"-N{n0 + rng.randrange(100, 20000)}"]))
+        binary = REF_DIR / "tpsieve_ref"
+
+        def one_twin(case):
+            name, args = case
+            with tempfile.TemporaryDirectory() as td:
+                cmd = [str(binary), *args, "-t2", "-m8192", "-c1000000", "-r1000000", "-q", "-fout.txt"]
+                r = subprocess.run(cmd, cwd=td, capture_output=True, text=True)
+                out = Path(td, "out.txt")
+                lines = [l.strip() for l in out.read_text().splitlines() if "|" in l] if out.exists() else []
+            m = FP_RE.search(r.stderr)
+            res = {"args": args, "binary": binary.name, "rc": r.returncode, "lines": sorted(lines),
+                   "unique": len(set(lines)), "total": len(lines)}
+            if m:
+                res["count"] = int(m.group(1))
+                res["sum"] = "0x" + m.group(2)
+            print(f"{name}: {len(lines)} lines rc={r.returncode}", flush=True)
+            return name, res
+
+        with ThreadPoolExecutor(max_workers=4) as ex:
+            out = dict(ex.map(one_twin, cases))
+        (HERE / "twin_cases.json").write_text(json.dumps(out, indent=1, sort_keys=True))
     if "kat" in which:
         kats = planted_kat49()
         out = []
