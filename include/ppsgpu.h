@@ -45,6 +45,15 @@ extern "C" {
 #define PPS_ERR_NOT_FOUND           (-305) /* unknown job id */
 #define PPS_ERR_CANCELLED           (-306)
 
+/* sign of a twin job: both k*2^n+1 and k*2^n-1 from one walk, as the
+   reference's twin build (tpsieve, -DSEARCH_TWIN: pps/app.c:1071-1107,
+   pps/appcu.cu:177-180, 741-767) reports them; k == 3 (mod 6) unless -M/-s
+   say otherwise.  Each factor carries its own c.  Twin jobs run on the
+   batched walk: pps_run_job, pps_run_batch and the serving loop take them;
+   the host-prime entry points and the appcu.h layer return
+   PPS_ERR_NOT_IMPLEMENTED. */
+#define PPS_SIGN_TWIN 2
+
 /* A job as the user states it; zero means "not given" exactly as in the
    reference options (-p -P -k -K -n -N -R -M -s -Q). */
 typedef struct {

@@ -417,8 +417,12 @@ __global__ void k_bchunkmap(const uint8_t* tables, const uint32_t* chunk_count, 
     if ((uint64_t)c0 + i < map_cap) chunk_seg[c0 + i] = s;
 }
 
+// Candidates carry their job slot in idx bits 0-30 and their side in bit 31
+// (1: k*2^n+1, 0: k*2^n-1), which a twin job needs per candidate.
+constexpr uint32_t SIDE_PROTH = BATCH_SIDE_PROTH;
+
 __device__ __forceinline__ void b_record(uint32_t klo, uint32_t khi, uint32_t n, uint32_t step, uint64_t p,
-                                         uint32_t job, const BJob& J, pps_hit* hits, uint32_t* hit_count,
+                                         uint32_t tag, const BJob& J, pps_hit* hits, uint32_t* hit_count,
                                          uint32_t hit_cap) {
   const uint32_t i = klo ? (uint32_t)(__ffs(klo) - 1) : (uint32_t)(31 + __ffs(khi));
   const uint64_t k = mk64(klo, khi) >> (i & 63u);
@@ -438,7 +442,7 @@ __device__ __forceinline__ void b_record(uint32_t klo, uint32_t khi, uint32_t n,
         h.p = p;
         h.k = k;
         h.n = n + i;
-        h.idx = job;
+        h.idx = tag;
         hits[pos] = h;
       }
     }
@@ -454,22 +458,34 @@ __device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t pl
 
 // One round: every lane walks one prime of the same job; flagged blocks of U
 // steps (and the partial last block) go to the warp's queue and are re-checked
-// exactly once the round's walks are done.
-template <bool S32, int U, bool WSH>
+// exactly once the round's walks are done.  A twin job (TW) walks K = 2^-n, the
+// -1 side's value, and tests p - K, the +1 side's, at the same step.
+template <bool S32, int U, bool WSH, bool TW>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
                                         uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
                                         uint32_t* hit_count, uint32_t hit_cap) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t s = S32 ? 32u : J.step;
   const uint32_t nsteps = J.nsteps, full = nsteps / (uint32_t)U;
+  const uint32_t tag = job | (J.proth == 1u ? SIDE_PROTH : 0u);  // the walked value's side
   qp[lane] = p;
   if (valid) {
     const uint32_t plo = lo32(p), phi = hi32(p);
     const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
     const uint64_t x = inv_pow2(J.nmin, p, ps);
-    const uint64_t K = J.proth ? p - x : x;
+    const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
     const uint32_t win_hi = J.win_hi, win_mask = J.win_mask, win_sh = J.win_sh;
+    // twin: p - K is below the window bound `lim` iff K > p - lim, and its low
+    // bits are zero iff K's equal p's
+    uint64_t tw_above = 0;
+    uint32_t tw_low = 0;
+    if (TW) {
+      // lim = 0 stands for 2^64 (every value inside)
+      const uint64_t lim = WSH ? (1ull << win_sh) : (win_hi == 0xffffffffu ? 0ull : ((uint64_t)win_hi + 1ull) << 32);
+      tw_above = (lim != 0ull && p > lim) ? p - lim : 0ull;
+      tw_low = plo & win_mask;
+    }
     for (uint32_t b = 0; b < full; ++b) {
       bool f = false;
 #pragma unroll
@@ -480,6 +496,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
           f |= (__funnelshift_rc(klo, khi, win_sh) == 0u) | ((klo & win_mask) == 0u);
         else
           f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
+        if (TW) f |= (mk64(klo, khi) > tw_above) | ((klo & win_mask) == tw_low);
         b_step<S32>(klo, khi, plo, phi, pinv_s, s);
       }
       if (f) {
@@ -510,14 +527,18 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
         K = qk[owner];
       } else {
         const uint64_t x = inv_pow2(n0, op, ops);
-        K = J.proth ? op - x : x;
+        K = J.proth == 1u ? op - x : x;
       }
       uint32_t klo = lo32(K), khi = hi32(K);
       const uint32_t oplo = lo32(op), ophi = hi32(op);
       const uint32_t opinv = S32 ? lo32(ops) : (lo32(ops) << (32u - s));
 #pragma unroll 1
       for (uint32_t u = 0; u < nblk; ++u) {
-        b_record(klo, khi, n0 + s * u, s, op, job, J, hits, hit_count, hit_cap);
+        b_record(klo, khi, n0 + s * u, s, op, tag, J, hits, hit_count, hit_cap);
+        if (TW) {
+          const uint64_t v = op - mk64(klo, khi);
+          b_record(lo32(v), hi32(v), n0 + s * u, s, op, job | SIDE_PROTH, J, hits, hit_count, hit_cap);
+        }
         b_step<S32>(klo, khi, oplo, ophi, opinv, s);
       }
     }
@@ -525,11 +546,15 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
     const uint32_t plo = lo32(p), phi = hi32(p);
     const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
     const uint64_t x = inv_pow2(J.nmin, p, ps);
-    const uint64_t K = J.proth ? p - x : x;
+    const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
 #pragma unroll 1
     for (uint32_t t = 0; t < nsteps; ++t) {
-      b_record(klo, khi, J.nmin + s * t, s, p, job, J, hits, hit_count, hit_cap);
+      b_record(klo, khi, J.nmin + s * t, s, p, tag, J, hits, hit_count, hit_cap);
+      if (TW) {
+        const uint64_t v = p - mk64(klo, khi);
+        b_record(lo32(v), hi32(v), J.nmin + s * t, s, p, job | SIDE_PROTH, J, hits, hit_count, hit_cap);
+      }
       b_step<S32>(klo, khi, plo, phi, pinv_s, s);
     }
   }
@@ -570,21 +595,24 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
       const bool valid = r + lane < count;
       const uint64_t pi = first + r + (valid ? lane : 0u);
       const uint64_t p = P[pi], ps = Pinv[pi];
+#define PPS_BROUND(S32_, WSH_, TW_)                                                                     \
+  b_round<S32_, U, WSH_, TW_>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, \
+                              hit_count, hit_cap)
+      const bool wsh = J.win_sh < 32u, tw = J.proth == 2u;
       if (J.step == 32) {
-        if (J.win_sh < 32u)
-          b_round<true, U, true>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
-                                 hit_count, hit_cap);
-        else
-          b_round<true, U, false>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
-                                  hit_count, hit_cap);
+        if (wsh) {
+          if (tw) PPS_BROUND(true, true, true); else PPS_BROUND(true, true, false);
+        } else {
+          if (tw) PPS_BROUND(true, false, true); else PPS_BROUND(true, false, false);
+        }
       } else {
-        if (J.win_sh < 32u)
-          b_round<false, U, true>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
-                                  hit_count, hit_cap);
-        else
-          b_round<false, U, false>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits,
-                                   hit_count, hit_cap);
+        if (wsh) {
+          if (tw) PPS_BROUND(false, true, true); else PPS_BROUND(false, true, false);
+        } else {
+          if (tw) PPS_BROUND(false, false, true); else PPS_BROUND(false, false, false);
+        }
       }
+#undef PPS_BROUND
     }
   }
 }
@@ -600,7 +628,8 @@ __global__ void k_bfilter(const pps_hit* hits, const uint32_t* d_nhits, uint32_t
   if (nh > hit_cap) nh = hit_cap;
   for (uint32_t h = warp; h < nh; h += nwarps) {
     const pps_hit x = hits[h];
-    const BJob J = jobs[x.idx];
+    const BJob J = jobs[x.idx & ~SIDE_PROTH];
+    const int32_t c = (x.idx & SIDE_PROTH) ? 1 : -1;
     bool ok = (x.k == J.kstep * (x.k / J.kstep) + J.koffset) && x.n >= J.nmin && x.n < J.nmax;
     if (ok) {
       bool div = false;
@@ -616,7 +645,7 @@ __global__ void k_bfilter(const pps_hit* hits, const uint32_t* d_nhits, uint32_t
             e >>= 1;
           }
           const uint32_t t = (kr * r) % q;
-          div = ((t + (uint32_t)((int32_t)q + J.sign)) % q) == 0u;
+          div = ((t + (uint32_t)((int32_t)q + c)) % q) == 0u;
         }
         if (__any_sync(0xffffffffu, div)) break;
       }
@@ -740,7 +769,7 @@ BJob make_job(const pps_job_params& jp) {
   J.nmax = jp.nmax;
   J.step = jp.step;
   J.nsteps = a.nsteps;
-  J.proth = a.proth;
+  J.proth = jp.sign == PPS_SIGN_TWIN ? 2u : a.proth;  // 2: both sides (twin)
   J.win_hi = a.win_hi;
   J.win_mask = a.win_mask;
   J.qmax = jp.qmax;
@@ -1038,12 +1067,7 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
       survivors->resize(at + nf);
       CU(cudaMemcpyAsync(survivors->data() + at, b->out.p, nf * sizeof(pps_hit), cudaMemcpyDeviceToHost, st));
       CU(cudaStreamSynchronize(st));
-      std::sort(survivors->begin() + at, survivors->end(), [](const pps_hit& x, const pps_hit& y) {
-        if (x.idx != y.idx) return x.idx < y.idx;
-        if (x.p != y.p) return x.p < y.p;
-        if (x.k != y.k) return x.k < y.k;
-        return x.n < y.n;
-      });
+      std::sort(survivors->begin() + at, survivors->end(), batch_hit_less);
     }
     CU(cudaEventSynchronize(e->ev[5]));
     float fms = 0;
@@ -1101,18 +1125,13 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
   CU(cudaEventRecord(e->ev[7], e->st));
   CU(cudaEventSynchronize(e->ev[7]));
   // survivors by job, each job's in (p, k, n) order
-  std::sort(surv.begin(), surv.end(), [](const pps_hit& x, const pps_hit& y) {
-    if (x.idx != y.idx) return x.idx < y.idx;
-    if (x.p != y.p) return x.p < y.p;
-    if (x.k != y.k) return x.k < y.k;
-    return x.n < y.n;
-  });
+  std::sort(surv.begin(), surv.end(), batch_hit_less);
   const size_t nf = surv.size();
   if (nout) *nout = nf;
   if (job_offsets) {
     size_t k = 0;
     for (size_t j = 0; j <= njobs; ++j) {
-      while (k < nf && surv[k].idx < j) ++k;
+      while (k < nf && batch_hit_slot(surv[k]) < j) ++k;
       job_offsets[j] = k;
     }
   }
@@ -1121,7 +1140,7 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
       out[i].p = surv[i].p;
       out[i].k = surv[i].k;
       out[i].n = surv[i].n;
-      out[i].c = jobs[surv[i].idx].sign;
+      out[i].c = batch_hit_sign(surv[i]);
     }
   }
   if (bst) {

@@ -53,10 +53,13 @@ extern "C" int pps_normalize(const pps_job_spec* in, pps_job_params* o) {
   memset(o, 0, sizeof *o);
   uint64_t pmin = in->pmin, pmax = in->pmax, kmin = in->kmin, kmax = in->kmax;
   uint32_t nmin = in->nmin, nmax = in->nmax, qmax = in->qmax;
-  uint32_t kstep = in->kstep ? in->kstep : 2u;    // pps/app.c:57
-  uint32_t koffset = in->koffset ? in->koffset : 1u;  // pps/app.c:58
   int32_t sign = in->sign ? in->sign : 1;
-  if (sign != 1 && sign != -1) return set_err(PPS_ERR_INVALID_PARAM, "sign must be +1 or -1");
+  if (sign != 1 && sign != -1 && sign != PPS_SIGN_TWIN)
+    return set_err(PPS_ERR_INVALID_PARAM, "sign must be +1, -1 or PPS_SIGN_TWIN");
+  const bool twin = sign == PPS_SIGN_TWIN;
+  // pps/app.c:53-58 KSTEP/KOFFSET: 6/3 in the twin (SEARCH_TWIN) build, else 2/1
+  uint32_t kstep = in->kstep ? in->kstep : (twin ? 6u : 2u);
+  uint32_t koffset = in->koffset ? in->koffset : (twin ? 3u : 1u);
   // main.c:916-931
   if (pmin < 3) pmin = 3;
   if (pmax > PMAX_MAX) pmax = PMAX_MAX;
@@ -88,6 +91,7 @@ extern "C" int pps_normalize(const pps_job_spec* in, pps_job_params* o) {
   if (nstep > nmax - nmin + 1) nstep = nmax - nmin + 1;
   if ((1ull << (64 - nstep)) > pmin)
     return set_err(PPS_ERR_INVALID_PARAM, "pmin is not large enough (or nmax is close to nmin)");
+  if (twin) nstep--;  // pps/appcu.cu:177-180: twin steps overlap by one n
   if (nstep >= 32 && nstep < 48 && (1ull << 32) <= pmin) nstep = 32;
   if (lg2u64(nmin) < 6) return set_err(PPS_ERR_INVALID_PARAM, "nmin too small at %u (must be at least 64)", nmin);
   // pps/appcu.cu:236-239
@@ -579,10 +583,41 @@ static int run_job_once(pps_engine* e, const pps_job_params* jp, pps_factor* out
   return rc;
 }
 
+// A twin job walks once for both sides on the batched form (one job, one
+// slot); its stats come from the batch's.
+static int run_twin_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap, size_t* nout,
+                        pps_job_stats* st) {
+  pps_batch_stats bst;
+  size_t n = 0, off[2];
+  const int rc = pps_run_batch(e, jp, 1, out, cap, &n, off, &bst);
+  if (nout) *nout = n;
+  if (st) {
+    memset(st, 0, sizeof *st);
+    st->primes = bst.primes;
+    st->prime_sum = bst.prime_sum;
+    st->raw_hits = bst.raw_hits;
+    st->factors = bst.factors;
+    st->steps = bst.steps;
+    st->batches = bst.waves;
+    st->variant = PPS_NUM_VARIANTS;  // the batched walk
+    st->total_ms = bst.total_ms;
+    st->filter_ms = bst.filter_ms;
+    st->walk_ms = bst.total_ms - bst.filter_ms;
+  }
+  return rc;
+}
+
+static int refuse_twin(const pps_job_params* jp) {
+  if (jp && jp->sign == PPS_SIGN_TWIN)
+    return set_err(PPS_ERR_NOT_IMPLEMENTED, "twin jobs run through pps_run_job / pps_run_batch");
+  return PPS_OK;
+}
+
 extern "C" int pps_run_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap,
                            size_t* nout, pps_job_stats* st) {
   if (!e || !jp) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
   if (jp->step < 1 || jp->step > 32 || jp->pmin <= (1ull << 32)) return set_err(PPS_ERR_INVALID_PARAM, "job not normalized");
+  if (jp->sign == PPS_SIGN_TWIN) return run_twin_job(e, jp, out, cap, nout, st);
   CU(cudaSetDevice(e->device));
   size_t hit_cap = 1u << 20, fac_cap = 1u << 18;
   for (int attempt = 0; attempt < 4; ++attempt) {
@@ -633,6 +668,7 @@ extern "C" int pps_check_primes_device(pps_engine* e, const pps_job_params* jp, 
                                        size_t np, pps_factor* out, size_t cap, size_t* nout,
                                        pps_job_stats* st) {
   if (!e || !jp || (!d_P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  if (int rc = refuse_twin(jp)) return rc;
   CU(cudaSetDevice(e->device));
   size_t hit_cap = 1u << 20, fac_cap = 1u << 18;
   for (int attempt = 0; attempt < 4; ++attempt) {
@@ -655,8 +691,9 @@ extern "C" int pps_check_primes_device(pps_engine* e, const pps_job_params* jp, 
 extern "C" int pps_check_primes(pps_engine* e, const pps_job_params* jp, const uint64_t* P, size_t np,
                                 pps_factor* out, size_t cap, size_t* nout, pps_job_stats* st) {
   if (!e || !jp || (!P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
-  CU(cudaSetDevice(e->device));
   int rc;
+  if ((rc = refuse_twin(jp))) return rc;
+  CU(cudaSetDevice(e->device));
   if ((rc = e->P.ensure(np ? np : 1))) return rc;
   if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
   return pps_check_primes_device(e, jp, e->P.p, np, out, cap, nout, st);
@@ -672,8 +709,9 @@ extern "C" int pps_check_primes_raw(pps_engine* e, const pps_job_params* jp, con
                                     pps_hit* out, size_t cap, size_t* nout) {
   if (!e || !jp || (!P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
   if (np > 0xffffffffull) return set_err(PPS_ERR_INVALID_PARAM, "too many primes for one call");
-  CU(cudaSetDevice(e->device));
   int rc;
+  if ((rc = refuse_twin(jp))) return rc;
+  CU(cudaSetDevice(e->device));
   if ((rc = e->P.ensure(np ? np : 1))) return rc;
   if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
   size_t hit_cap = std::max<size_t>(1u << 20, e->hits.n);

@@ -100,6 +100,16 @@ struct BatchPiece {
   uint64_t lo, hi;  // p in [lo, hi)
   uint32_t slot;
 };
+// A wave's candidates and survivors: idx = job slot | side bit (set: k*2^n+1).
+constexpr uint32_t BATCH_SIDE_PROTH = 0x80000000u;
+inline uint32_t batch_hit_slot(const pps_hit& h) { return h.idx & ~BATCH_SIDE_PROTH; }
+inline int32_t batch_hit_sign(const pps_hit& h) { return (h.idx & BATCH_SIDE_PROTH) ? 1 : -1; }
+inline bool batch_hit_less(const pps_hit& x, const pps_hit& y) {  // (slot, p, k, n)
+  if (batch_hit_slot(x) != batch_hit_slot(y)) return batch_hit_slot(x) < batch_hit_slot(y);
+  if (x.p != y.p) return x.p < y.p;
+  if (x.k != y.k) return x.k < y.k;
+  return x.n < y.n;
+}
 uint32_t batch_max_slots();
 uint64_t batch_wave_segments();          // segments one wave holds
 uint64_t batch_piece_segments(uint64_t lo, uint64_t hi);

@@ -96,6 +96,7 @@ extern "C" int pps_check_primes_noalloc(const pps_job_params* jp, const uint64_t
     return fail(PPS_ERR_INVALID_PARAM, "null argument");
   if (jp->step < 1 || jp->step > 32 || jp->pmin <= (1ull << 32))
     return fail(PPS_ERR_INVALID_PARAM, "job not normalized (use pps_normalize)");
+  if (jp->sign == PPS_SIGN_TWIN) return fail(PPS_ERR_NOT_IMPLEMENTED, "twin jobs run through pps_run_job");
   if (np > PPS_NOALLOC_MAX_PRIMES)
     return fail(PPS_ERR_INVALID_PARAM, "%zu primes exceed the limit of %u per call; split the list",
                 np, (unsigned)PPS_NOALLOC_MAX_PRIMES);

@@ -164,9 +164,9 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
     std::unordered_map<uint32_t, JobRec*> by_slot;
     for (JobRec* j : in_wave) by_slot[j->slot] = j;
     for (const pps_hit& h : surv) {
-      auto it = by_slot.find(h.idx);
+      auto it = by_slot.find(batch_hit_slot(h));
       if (it == by_slot.end()) continue;
-      it->second->factors.push_back(pps_factor{h.p, h.k, h.n, it->second->jp.sign});
+      it->second->factors.push_back(pps_factor{h.p, h.k, h.n, batch_hit_sign(h)});
     }
     for (JobRec* j : finishing) {
       const int crc = batch_job_counts(e, j->slot, 1, &j->primes, &j->sum);

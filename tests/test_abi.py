@@ -73,7 +73,7 @@ def test_normalize_matches_oracle_random(pps, ora):
             kmax=rng.choice([0, rng.randrange(1, 20000), rng.randrange(1, 1 << 40)]),
             nmin=rng.choice([0, rng.randrange(1, 300), rng.randrange(1, 1 << 22)]),
             nmax=rng.choice([0, rng.randrange(1, 1 << 22)]),
-            sign=rng.choice([1, -1]),
+            sign=rng.choice([1, -1, 2]),  # 2: twin
             kstep=rng.choice([0, 2, 6]), koffset=rng.choice([0, 1, 3]),
             qmax=rng.choice([0, 0, rng.randrange(61, 1 << 20)]))
         try:
