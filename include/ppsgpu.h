@@ -60,7 +60,7 @@ typedef struct {
   uint64_t pmin, pmax;
   uint64_t kmin, kmax;
   uint32_t nmin, nmax;
-  int32_t  sign;      /* +1 Proth (default when 0), -1 Riesel (-R) */
+  int32_t  sign;      /* +1 Proth (default when 0), -1 Riesel (-R), PPS_SIGN_TWIN both */
   uint32_t kstep;     /* -M, default 2 */
   uint32_t koffset;   /* -s, default 1 */
   uint32_t qmax;      /* -Q, default sqrt(pmax) */
