@@ -28,10 +28,14 @@ class Params(ctypes.Structure):
                 ("nmin", ctypes.c_uint32), ("nmax", ctypes.c_uint32),
                 ("c", ctypes.c_int32), ("kstep", ctypes.c_uint32),
                 ("koffset", ctypes.c_uint32), ("qmax", ctypes.c_uint32),
-                ("nstep", ctypes.c_uint32)]
+                ("nstep", ctypes.c_uint32), ("pad0", ctypes.c_uint32),
+                ("input_keys", ctypes.c_void_p), ("ninput", ctypes.c_uint64),
+                ("input_width", ctypes.c_uint64)]
+    _INPUT_FIELDS = ("pad0", "input_keys", "ninput", "input_width")
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        """The job's parameters (the input-file fields excluded)."""
+        return {f: getattr(self, f) for f, _ in self._fields_ if f not in self._INPUT_FIELDS}
 
 
 def build() -> None:
@@ -186,3 +190,122 @@ def parse_line(line: str) -> tuple[int, int, int, int]:
         return p, int(kpart), int(n), int(c)
     n, c = rest.split("-")
     return p, int(kpart), int(n), -int(c)
+
+
+# ---------------------------------------------------------------- input files
+
+ERR_SCANF = -140  # pps/app.h:69
+
+
+class InputFile:
+    """A sieve file as the reference reads it (pps/app.c:190-517): NewPGen
+    ("p0:P:x:2:c" then "k n" lines) or ABCD ("ABCD k*2^$a+1 [n0]" then n
+    deltas).  records: (k, n) in file order; k0..k1, n0..n1 the scan's extents
+    (n1 one past the largest n, pps/app.c:319)."""
+
+    def __init__(self, fmt: str, sign: int, records: list[tuple[int, int]]):
+        self.format, self.sign, self.records = fmt, sign, records
+        ks = [k for k, _ in records]
+        ns = [n for _, n in records]
+        self.k0, self.k1 = min(ks), max(ks)
+        self.n0, self.n1 = min(ns), max(ns) + 1
+
+
+def read_input(path, detect: bool = True) -> InputFile:
+    """Format detection and parsing (pps/app.c:208-231 headers, 242-309 scan,
+    349-517 read).  The reference detects the format only while scanning (when
+    one of kmin, kmax, nmin, nmax is not given); otherwise it reads the file as
+    ABCD (pps/app.c:97), and a NewPGen file is an invalid header."""
+    import re
+
+    text = open(path).read().splitlines()
+    m = re.match(r"ABCD (\d+)\*2\^\$a([+-])1 \[(\d+)\]", text[0]) if text else None
+    if not m and not detect:
+        raise OracleError(ERR_SCANF)
+    if m:
+        recs, k, n = [], int(m.group(1)), int(m.group(3))
+        sign = 1 if m.group(2) == "+" else -1
+        recs.append((k, n))
+        for line in text[1:]:
+            h = re.match(r"\s*ABCD (\d+)\*2\^\$a[+-]1 \[(\d+)\]", line)
+            if h:
+                k, n = int(h.group(1)), int(h.group(2))
+                recs.append((k, n))
+                continue
+            d = re.match(r"(\d+)", line)
+            if not d:
+                continue  # blank line
+            n += int(d.group(1))
+            recs.append((k, n))
+        return InputFile("abcd", sign, recs)
+    m = re.match(r"\s*(\d+):P:.:2:(-?\d+)", text[0]) if text else None
+    if not m or int(m.group(2)) not in (1, -1, 255, 257):
+        raise OracleError(ERR_SCANF)
+    c = int(m.group(2))
+    sign = 1 if c in (1, 257) else -1  # (char) of the header's c
+    recs = []
+    for line in text[1:]:
+        f = line.split()
+        if len(f) < 2:
+            break
+        recs.append((int(f[0]), int(f[1])))
+    if not recs:
+        raise OracleError(ERR_SCANF)  # "Invalid line 2"
+    return InputFile("newpgen", sign, recs)
+
+
+def input_spec(inp: InputFile, spec: dict) -> dict:
+    """The scan's effect on the job (pps/app.c:661-663, 335-346): only when one
+    of kmin, kmax, nmin, nmax is not given; the file's side is taken then."""
+    spec = dict(spec)
+    if all(spec.get(f) for f in ("kmin", "kmax", "nmin", "nmax")):
+        return spec
+    spec["sign"] = inp.sign
+    spec["kmin"] = max(spec.get("kmin") or 0, inp.k0)
+    if not spec.get("kmax") or spec["kmax"] > inp.k1:
+        spec["kmax"] = inp.k1
+    spec["nmin"] = max(spec.get("nmin") or 0, inp.n0)
+    if not spec.get("nmax") or spec["nmax"] > inp.n1:
+        spec["nmax"] = inp.n1
+    return spec
+
+
+def input_keys(inp: InputFile, params: Params) -> np.ndarray:
+    """The file's bitmap (pps/app.c:726-737, 383-392, 440-478) as sorted keys
+    (n - nmin) * width + (k - kmin) / kstep.  NewPGen lines must have
+    k == koffset (mod kstep) (pps/app.c:385-389).  Entries whose bit would fall
+    outside the reference's bitmap are left out."""
+    kstep, koffset = params.kstep, params.koffset
+    width = (params.kmax - params.kmin) // kstep + 1
+    b0 = (params.kmin - koffset) // kstep
+    keys = set()
+    for k, n in inp.records:
+        if inp.format == "newpgen":
+            if k % kstep != koffset:
+                raise OracleError(ERR_SCANF)
+            if not (params.kmin <= k <= params.kmax):
+                continue
+            bit = k // kstep - b0
+        else:
+            if k < params.kmin:
+                continue
+            bit = (k - params.kmin) // kstep
+            if bit >= width:
+                continue
+        if params.nmin <= n <= params.nmax:
+            keys.add((n - params.nmin) * width + bit)
+    return np.array(sorted(keys), dtype=np.uint64)
+
+
+def attach_input(params: Params, keys: np.ndarray) -> Params:
+    """Use the file as the output rule of `params` (keys stay referenced)."""
+    params._keys = keys
+    params.input_keys = keys.ctypes.data if len(keys) else None
+    params.ninput = len(keys)
+    params.input_width = (params.kmax - params.kmin) // params.kstep + 1
+    if not len(keys):
+        # an empty file set reports nothing: a key no candidate can have
+        params._keys = np.array([np.iinfo(np.uint64).max], dtype=np.uint64)
+        params.input_keys = params._keys.ctypes.data
+        params.ninput = 1
+    return params

@@ -180,6 +180,17 @@ int ppo_test_factor(const ppo_params *pp, uint64_t k, uint32_t n, int32_t c)
   uint64_t b = k / pp->kstep;
   if (k != pp->kstep * b + pp->koffset) return 0;
   if (n < pp->nmin || n >= pp->nmax) return 0;
+  if (pp->input_keys) {
+    /* pps/app.c:180-183: the bit of (k, n) in the input file's bitmap */
+    if (k < pp->kmin || k > pp->kmax) return 0;
+    const uint64_t key = (uint64_t)(n - pp->nmin) * pp->input_width + (k - pp->kmin) / pp->kstep;
+    uint64_t lo = 0, hi = pp->ninput;
+    while (lo < hi) {
+      const uint64_t mid = lo + (hi - lo) / 2;
+      if (pp->input_keys[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo < pp->ninput && pp->input_keys[lo] == key;
+  }
   return ppo_small_factor(k, n, c) == 0;
 }
 

@@ -46,6 +46,13 @@ typedef struct {
   uint32_t kstep, koffset;
   uint32_t qmax;         /* largest sieving prime bound actually used */
   uint32_t nstep;        /* n values covered per walk step */
+  /* Input sieve file (-i) as the output rule (pps/app.c:180-183): when
+     input_keys is set, a line is printed iff its (k, n) is in the file, with
+     no small-prime filter.  Keys (n - nmin) * input_width + (k - kmin) / kstep,
+     ascending; input_width = (kmax - kmin) / kstep + 1. */
+  uint32_t pad0;
+  const uint64_t *input_keys;
+  uint64_t ninput, input_width;
 } ppo_params;
 
 typedef struct {

@@ -164,6 +164,86 @@ def planted_kat49(max_found: int = 8, seed: int = 7) -> list[dict]:
     return found
 
 
+INPUTS = HERE / "inputs"
+SMALL_Q = (3, 5, 7, 11, 13, 17, 19, 23, 29)
+
+
+def _survivors(kmin: int, kmax: int, nmin: int, nmax: int, c: int) -> list[tuple[int, int]]:
+    """(k, n) with k odd, nmin <= n <= nmax, k*2^n+c free of the primes below 30:
+    a stand-in for the output of a sieving program such as NewPGen."""
+    out = []
+    for k in range(kmin | 1, kmax + 1, 2):
+        for n in range(nmin, nmax + 1):
+            if all((k * pow(2, n, q) + c) % q for q in SMALL_Q):
+                out.append((k, n))
+    return out
+
+
+def write_newpgen(path: Path, pairs, c: int) -> None:
+    """NewPGen format as pps/app.c:221-230 reads it: "p0:P:x:2:c" then "k n" lines."""
+    lines = [f"30:P:1:2:{c}"] + [f"{k} {n}" for k, n in sorted(pairs)]
+    path.write_text("\n".join(lines) + "\n")
+
+
+def write_abcd(path: Path, pairs, c: int) -> None:
+    """ABCD format as pps/app.c:213-218 and 405-500 read it: per k a header
+    "ABCD k*2^$a+1 [n0]" then one n delta per line."""
+    by_k: dict[int, list[int]] = {}
+    for k, n in sorted(pairs):
+        by_k.setdefault(k, []).append(n)
+    out = []
+    sign = "+" if c > 0 else "-"
+    for k, ns in by_k.items():
+        out.append(f"ABCD {k}*2^$a{sign}1 [{ns[0]}] // sieved to 30")
+        out += [str(b - a) for a, b in zip(ns, ns[1:])]
+    path.write_text("\n".join(out) + "\n")
+
+
+def make_input_cases() -> None:
+    """Synthetic sieve files in both formats and both signs, and the reference's
+    own output when given each with -i (bitmap output rule, pps/app.c:180-183)."""
+    INPUTS.mkdir(exist_ok=True)
+    files = {}
+    for c in (1, -1):
+        pairs = _survivors(3, 99, 1000, 1999, c)
+        tag = "proth" if c > 0 else "riesel"
+        write_newpgen(INPUTS / f"newpgen_{tag}.txt", pairs, c)
+        write_abcd(INPUTS / f"abcd_{tag}.txt", pairs, c)
+        files[tag] = len(pairs)
+    print("input files:", files, flush=True)
+    lo = 5 * 10**10
+    cases = []
+    for fmt in ("newpgen", "abcd"):
+        for tag in ("proth", "riesel"):
+            f = f"{fmt}_{tag}.txt"
+            # ranges from the file (the reference's scan_input_file, pps/app.c:190-347)
+            cases.append((f"in_{fmt}_{tag}", f, [f"-p{lo}", f"-P{lo + 25 * 10**8}"]))
+    # k/n all given: no scan, so no format detection either: the file is read as
+    # ABCD (pps/app.c:97), and a NewPGen file is refused (ERR_SCANF, exit 116)
+    cases.append(("in_newpgen_proth_given", "newpgen_proth.txt",
+                  [f"-p{lo}", f"-P{lo + 25 * 10**8}", "-k11", "-K61", "-n1200", "-N1800"]))
+    # ABCD against given ranges, -R by option.  The k range covers the file's:
+    # pps/app.c:440-447 does not check k, so a k below kmin writes outside the
+    # reference's bitmap (it crashed on that here), and headers' n are unchecked
+    # above nmax; both are left out of the fixtures.
+    cases.append(("in_abcd_riesel_given", "abcd_riesel.txt",
+                  [f"-p{lo}", f"-P{lo + 25 * 10**8}", "-k3", "-K99", "-n1200", "-N1800", "-R"]))
+    # a partial override: kmax given, the rest from the file
+    cases.append(("in_abcd_proth_kmax", "abcd_proth.txt", [f"-p{lo}", f"-P{lo + 25 * 10**8}", "-K51"]))
+
+    def one(case):
+        name, f, args = case
+        r = run_ref([*args, f"-i{INPUTS / f}"], threads=2)
+        r["args"] = args
+        r["input"] = f
+        print(f"{name}: {r['total']} lines rc={r['rc']}", flush=True)
+        return name, r
+
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        out = dict(ex.map(one, cases))
+    (HERE / "input_cases.json").write_text(json.dumps(out, indent=1, sort_keys=True))
+
+
 def main() -> None:
     if not REF_BIN.exists() or not REF_FIXED.exists():
         sys.exit("build the reference first: make -C oracle ref")
@@ -260,6 +340,8 @@ def main() -> None:
         with ThreadPoolExecutor(max_workers=4) as ex:
             out = dict(ex.map(one_twin, cases))
         (HERE / "twin_cases.json").write_text(json.dumps(out, indent=1, sort_keys=True))
+    if "input" in which:
+        make_input_cases()
     if "kat" in which:
         kats = planted_kat49()
         out = []
