@@ -37,6 +37,7 @@ extern "C" {
 #define PPS_ERR_INSUFFICIENT_RESOURCE (-198)
 #define PPS_ERR_NOT_IMPLEMENTED     (-150)
 #define PPS_ERR_FOPEN               (-108)
+#define PPS_ERR_SCANF               (-140) /* bad input sieve file (pps/app.h:69) */
 #define PPS_ERR_CUDA                (-300) /* a CUDA runtime call failed */
 #define PPS_ERR_NO_DEVICE           (-301) /* no usable GPU */
 #define PPS_ERR_OVERFLOW            (-302) /* caller's output buffer too small */
@@ -173,6 +174,43 @@ int pps_measure_imad_peak(pps_engine *e, double *mults_per_sec);
 
 /* Number of the engine's own kernels launched so far. */
 uint64_t pps_engine_launches(const pps_engine *e);
+
+/* ---- Input sieve files (-i; pps/app.c:190-517 read them, pps/app.c:180-183
+   applies them).  A file lists the (k, n) still to be tested, in NewPGen
+   format ("p0:P:x:2:c" then "k n" lines) or ABCD format ("ABCD k*2^$a+1 [n0]"
+   then n deltas).  With a file the output rule is the file: a factor is
+   reported iff its (k, n) is in the file (and k == koffset mod kstep, n in
+   [nmin, nmax)); the small-prime filter is not applied.
+
+   pps_input_read parses a file against the job as the user stated it.  When
+   one of spec->kmin, kmax, nmin, nmax is 0 it scans the file like
+   scan_input_file (pps/app.c:190-347): it detects the format, takes the sign
+   from the header and fills kmin/kmax/nmin/nmax from the file's extents
+   (nmax one past the largest n).  When all four are given the file is read as
+   ABCD without a scan (pps/app.c:97), so a NewPGen file is refused.  Errors:
+   PPS_ERR_FOPEN, PPS_ERR_SCANF.  Entries the reference would write outside its
+   bitmap (an ABCD k below kmin or past kmax; n past nmax) are ignored. */
+typedef struct pps_input pps_input;
+
+typedef struct {
+  int32_t format;          /* 1 NewPGen, 2 ABCD (the reference's FORMAT_ values) */
+  int32_t sign;            /* the header's side */
+  uint64_t records;        /* (k, n) entries read */
+  uint64_t k0, k1;         /* smallest and largest k */
+  uint32_t n0, n1;         /* smallest n, one past the largest */
+} pps_input_info;
+
+int pps_input_read(const char *path, pps_job_spec *spec, pps_input **out);
+int pps_input_get_info(const pps_input *in, pps_input_info *info);
+void pps_input_free(pps_input *in);
+
+/* Use `in` as the output rule of this engine's pps_run_job and
+   pps_check_primes* calls (NULL: back to the small-prime filter).  The engine
+   keeps the pointer: `in` must outlive its use.  The file's table for a job is
+   built at the job's first call (PPS_ERR_SCANF when a NewPGen line has
+   k != koffset mod kstep, pps/app.c:385-389).  The batched form and the
+   serving loop always apply the small-prime filter. */
+int pps_engine_set_input(pps_engine *e, const pps_input *in);
 
 /* ---- Batched persistent form (no single counterpart in the reference, which
    runs one range per process, main.c:887-1266).  Many normalised jobs --

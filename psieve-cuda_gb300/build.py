@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 LIB_SOURCES = ["pps_kernels.cu", "pps_engine.cu", "pps_batch.cu", "pps_server.cu",
-               "pps_noalloc.cu"]
+               "pps_noalloc.cu", "pps_input.cu"]
 COMPAT_SOURCES = ["appcu_compat.cu"]
 
 

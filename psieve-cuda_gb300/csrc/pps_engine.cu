@@ -118,6 +118,7 @@ static void free_engine(pps_engine* e) {
   cudaSetDevice(e->device);
   e->base_q.release();
   e->seed_q.release();
+  e->in_keys.release();
   e->bitmap.release();
   e->seg_count.release();
   e->seg_off.release();
@@ -478,6 +479,34 @@ static bool factor_less(const pps_factor& x, const pps_factor& y) {
   return x.c < y.c;
 }
 
+// The input file's key table for this job (built when the job's ranges change).
+static int ensure_input_keys(pps_engine* e, const pps_job_params* jp) {
+  if (!e->input) return PPS_OK;
+  const pps_job_params& b = e->in_job;
+  if (e->in_built && b.kmin == jp->kmin && b.kmax == jp->kmax && b.kstep == jp->kstep &&
+      b.koffset == jp->koffset && b.nmin == jp->nmin && b.nmax == jp->nmax)
+    return PPS_OK;
+  std::vector<uint64_t> keys;
+  uint64_t width = 0;
+  int rc = input_keys_for_job(e->input, jp, &keys, &width);
+  if (rc) return rc;
+  if ((rc = e->in_keys.ensure(std::max<size_t>(keys.size(), 1)))) return rc;
+  if (!keys.empty())
+    CU(cudaMemcpy(e->in_keys.p, keys.data(), keys.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+  e->in_n = keys.size();
+  e->in_width = width;
+  e->in_job = *jp;
+  e->in_built = true;
+  return PPS_OK;
+}
+
+extern "C" int pps_engine_set_input(pps_engine* e, const pps_input* in) {
+  if (!e) return set_err(PPS_ERR_INVALID_PARAM, "null engine");
+  e->input = in;
+  e->in_built = false;
+  return PPS_OK;
+}
+
 // Filter the raw hits accumulated in e->hits and copy the factors out.
 static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap, size_t* nout,
                       pps_job_stats* st, uint32_t* raw_hits_out, bool* overflow) {
@@ -489,6 +518,7 @@ static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, 
     *overflow = true;
     return PPS_OK;
   }
+  if (int rc = ensure_input_keys(e, jp)) return rc;
   FilterArgs f;
   f.hits = e->hits.p;
   f.d_nhits = e->counters.p;
@@ -503,6 +533,13 @@ static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, 
   f.out = e->factors.p;
   f.out_count = e->counters.p + 1;
   f.out_cap = (uint32_t)std::min<size_t>(e->factors.n, 0xffffffffu);
+  if (e->input) {
+    f.in_keys = e->in_keys.p;
+    f.in_n = e->in_n;
+    f.in_width = e->in_width;
+    f.kmin = jp->kmin;
+    f.kmax = jp->kmax;
+  }
   CU(cudaEventRecord(e->ev[4], e->st));
   if (raw) {
     CU(launch_filter(f, raw, e->st));

@@ -80,7 +80,19 @@ struct pps_engine {
   uint64_t* h_pinned = nullptr;  // 16 words of pinned host scratch
 
   BatchState* batch = nullptr;  // state of the batched persistent form
+
+  // input sieve file as the output rule (pps_engine_set_input), and its key
+  // table for the job it was last built for
+  const pps_input* input = nullptr;
+  DevBuf<uint64_t> in_keys;
+  uint64_t in_n = 0, in_width = 0;
+  bool in_built = false;
+  pps_job_params in_job{};
 };
+
+// Sorted bit numbers of the input file's bitmap for one job (pps_input.cu).
+int input_keys_for_job(const pps_input* in, const pps_job_params* jp, std::vector<uint64_t>* keys,
+                       uint64_t* width);
 
 struct BaseTable {
   uint32_t nq, nq_tiny, nq_seg;

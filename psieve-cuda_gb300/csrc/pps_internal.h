@@ -85,6 +85,11 @@ struct FilterArgs {
   pps_factor* out;
   uint32_t* out_count;
   uint32_t out_cap;
+  // input sieve file as the output rule instead of small_q: sorted keys
+  // (n - nmin) * in_width + (k - kmin) / kstep (pps/app.c:180-183)
+  const uint64_t* in_keys = nullptr;
+  uint64_t in_n = 0, in_width = 0;
+  uint64_t kmin = 0, kmax = 0;
 };
 cudaError_t launch_filter(const FilterArgs& a, uint32_t max_hits, cudaStream_t st);
 

@@ -569,7 +569,19 @@ __global__ void k_filter(FilterArgs a) {
   for (uint32_t h = warp; h < nh; h += nwarps) {
     const pps_hit x = a.hits[h];
     bool ok = (x.k == a.kstep * (x.k / a.kstep) + a.koffset) && x.n >= a.nmin && x.n < a.nmax;
-    if (ok) {
+    if (ok && a.in_keys) {
+      // the input file's bit of (k, n), every lane the same search
+      ok = x.k >= a.kmin && x.k <= a.kmax;
+      if (ok) {
+        const uint64_t key = (uint64_t)(x.n - a.nmin) * a.in_width + (x.k - a.kmin) / a.kstep;
+        uint64_t lo = 0, hi = a.in_n;
+        while (lo < hi) {
+          const uint64_t mid = lo + (hi - lo) / 2;
+          if (a.in_keys[mid] < key) lo = mid + 1; else hi = mid;
+        }
+        ok = lo < a.in_n && a.in_keys[lo] == key;
+      }
+    } else if (ok) {
       bool div = false;
       for (uint32_t base = 0; base < a.nsmall; base += 32u) {
         const uint32_t i = base + lane;

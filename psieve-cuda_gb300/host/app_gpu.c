@@ -34,7 +34,7 @@ char *bmprefix();
 #define FACTORS_FILENAME_DEFAULT "ppfactors.txt"
 #define ERR_FOPEN (-108)
 #define ERR_INVALID_PARAM (-178)
-#define ERR_NOT_IMPLEMENTED (-150)
+#define ERR_SCANF (-140)
 #define MAX_APP_THREADS 64
 #define BATCH_BLOCK 128u /* pps/appcu.h:14 */
 
@@ -45,6 +45,7 @@ int search_proth = 1;
 struct n_subsection *thread_subsections;
 
 static const char *input_filename = NULL;
+static pps_input *input_set = NULL;  /* -i: the file as the output rule */
 static const char *factors_filename = NULL;
 static FILE *factors_file = NULL;
 static unsigned int factor_count = 0;
@@ -168,7 +169,7 @@ int app_parse_option(int opt, char *arg, const char *source)
 void app_help(void)
 {
   printf("-f --factors=FILE  Write factors to FILE (default `%s')\n", FACTORS_FILENAME_DEFAULT);
-  printf("-i --input=FILE    Read initial sieve from FILE (not supported by this build)\n");
+  printf("-i --input=FILE    Read initial sieve from FILE\n");
   printf("-M --modulus       (Default 2)\n");
   printf("-s --modshift      Print only k's == s mod M. Default 1, or M/2\n");
   printf("-k --kmin=K0\n");
@@ -185,10 +186,6 @@ void app_init(void)
 {
   pps_job_spec spec;
   print_factors = quiet_opt ? 0 : 1;
-  if (input_filename != NULL) {
-    bmsg("Input sieve files (-i) are not supported by this build\n");
-    bexit(ERR_NOT_IMPLEMENTED);
-  }
   memset(&spec, 0, sizeof spec);
   spec.pmin = pmin;
   spec.pmax = pmax;
@@ -199,6 +196,20 @@ void app_init(void)
   spec.sign = search_proth;
   spec.kstep = kstep;
   spec.koffset = koffset;
+  if (input_filename != NULL) {
+    /* pps/app.c:661-663 and 726-738: the file fills the bounds the command
+       line left open, and becomes the output rule */
+    const int rc = pps_input_read(input_filename, &spec, &input_set);
+    if (rc == PPS_ERR_FOPEN) {
+      perror(input_filename);
+      bexit(ERR_FOPEN);
+    }
+    if (rc != PPS_OK) {
+      fprintf(stderr, "%s%s\n", bmprefix(), pps_last_error());
+      bexit(ERR_SCANF);
+    }
+    search_proth = spec.sign;
+  }
   if (pps_normalize(&spec, &job) != PPS_OK) {
     char msg[600];
     snprintf(msg, sizeof msg, "%s\n", pps_last_error());
@@ -234,6 +245,7 @@ unsigned int app_thread_init(int th)
     fprintf(stderr, "%sGPU %d not usable: %s\n", bmprefix(), dev, pps_last_error());
     return 0;
   }
+  if (input_set) pps_engine_set_input(t->eng, input_set);
   if (cnt == 0) cnt = 2048;
   else if (cnt < BATCH_BLOCK) cnt *= BATCH_BLOCK;
   else cnt -= cnt % BATCH_BLOCK;
@@ -386,4 +398,6 @@ void app_fini(uint64_t pstop)
   printf("Found %u factor%s\n", factor_count, (factor_count == 1) ? "" : "s");
   free(thread_subsections);
   thread_subsections = NULL;
+  pps_input_free(input_set);
+  input_set = NULL;
 }

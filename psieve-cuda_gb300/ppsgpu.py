@@ -111,6 +111,45 @@ class ServerStats(ctypes.Structure):
 
 
 PPS_JOB_QUEUED, PPS_JOB_RUNNING, PPS_JOB_DONE, PPS_JOB_FAILED = 0, 1, 2, 3
+PPS_ERR_FOPEN = -108
+PPS_ERR_SCANF = -140
+
+
+class InputInfo(ctypes.Structure):
+    _fields_ = [("format", ctypes.c_int32), ("sign", ctypes.c_int32),
+                ("records", ctypes.c_uint64), ("k0", ctypes.c_uint64), ("k1", ctypes.c_uint64),
+                ("n0", ctypes.c_uint32), ("n1", ctypes.c_uint32)]
+
+
+class InputFile:
+    """An input sieve file (pps_input_read).  `spec` is the job as stated,
+    completed from the file where a k or n bound was not given."""
+
+    def __init__(self, path, pmin=0, pmax=0, kmin=0, kmax=0, nmin=0, nmax=0, sign=1, kstep=0,
+                 koffset=0, qmax=0, lib=None):
+        self.lib = lib or load()
+        spec = JobSpec(pmin, pmax, kmin, kmax, nmin, nmax, sign, kstep, koffset, qmax)
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.pps_input_read(str(path).encode(), ctypes.byref(spec),
+                                                 ctypes.byref(h)))
+        self.h = h
+        self.spec = {f: getattr(spec, f) for f, _ in JobSpec._fields_}
+
+    def info(self) -> InputInfo:
+        info = InputInfo()
+        _check(self.lib, self.lib.pps_input_get_info(self.h, ctypes.byref(info)))
+        return info
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.pps_input_free(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PPSError(RuntimeError):
@@ -170,6 +209,10 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_job_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double,
                                         ctypes.c_void_p, ctypes.c_size_t, szp, P(JobResult)]),
         "pps_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(ServerStats)]),
+        "pps_input_read": (ctypes.c_int, [ctypes.c_char_p, P(JobSpec), P(ctypes.c_void_p)]),
+        "pps_input_get_info": (ctypes.c_int, [ctypes.c_void_p, P(InputInfo)]),
+        "pps_input_free": (None, [ctypes.c_void_p]),
+        "pps_engine_set_input": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -241,6 +284,11 @@ class Engine:
 
     def set_variant(self, v: int) -> None:
         _check(self.lib, self.lib.pps_engine_set_variant(self.h, v))
+
+    def set_input(self, inp: "InputFile | None") -> None:
+        """Use an input sieve file as the output rule (None: the small-prime filter)."""
+        self._input = inp  # keep it alive while the engine uses it
+        _check(self.lib, self.lib.pps_engine_set_input(self.h, inp.h if inp else None))
 
     def _call_factors(self, fn, *args, cap: int = 1 << 16):
         while True:

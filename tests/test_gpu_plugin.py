@@ -48,12 +48,44 @@ def test_plugin_factor_file(driver, tmp_path, ora, ref_cases, name):
     assert f"Found {n} factor{'' if n == 1 else 's'}" in r.stdout
 
 
-def test_plugin_rejects_input_file(driver, tmp_path):
+GOLDEN = ROOT / "tests" / "golden"
+
+
+@pytest.mark.parametrize("name", ["in_newpgen_proth", "in_abcd_riesel", "in_abcd_riesel_given",
+                                  "in_abcd_proth_kmax"])
+def test_plugin_input_file(driver, tmp_path, ora, name):
+    """-i: the factor file equals the reference's own run with the same file."""
+    import json
+
+    import math
+
+    case = json.loads((GOLDEN / "input_cases.json").read_text())[name]
+    spec = args_to_spec(case["args"])
+    # the first tenth of the fixture's p range (its lines there), to keep the prime file small
+    lo, hi = spec["pmin"], spec["pmin"] + (spec["pmax"] - spec["pmin"]) // 10
+    primes = ora.sieve_range(lo | 1, hi, math.isqrt(hi))
+    pf = tmp_path / "primes.bin"
+    primes.astype("<u8").tofile(pf)
+    ff = tmp_path / "factors.txt"
+    args = [a for a in case["args"] if not a.startswith(("-p", "-P"))]
+    r = subprocess.run([str(driver), str(pf), f"-p{lo}", f"-P{hi}", *args,
+                        f"-i{GOLDEN / 'inputs' / case['input']}", f"-f{ff}", "-m1"],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr
+    lines = sorted(l for l in ff.read_text().splitlines() if "|" in l) if ff.exists() else []
+    want = sorted(l for l in case["lines"] if int(l.split("|")[0]) < hi)
+    assert lines == want and len(case["lines"]) > 0
+
+
+def test_plugin_input_file_refused_like_reference(driver, tmp_path):
+    """All k/n bounds given: the file is read as ABCD, so a NewPGen file is a
+    bad header (the reference exits with ERR_SCANF)."""
     pf = tmp_path / "p.bin"
     pf.write_bytes(b"")
-    r = subprocess.run([str(driver), str(pf), "-p1000000000000", "-P1000000100000", "-k1201",
-                        "-K9999", "-n2000", "-N3000", "-iabcd.txt"], capture_output=True, text=True)
-    assert r.returncode == 3 and "bexit(-150)" in r.stderr
+    r = subprocess.run([str(driver), str(pf), "-p50000000000", "-P50001000000", "-k11", "-K61",
+                        "-n1200", "-N1800", f"-i{GOLDEN / 'inputs' / 'newpgen_proth.txt'}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 3 and "bexit(-140)" in r.stderr
 
 
 def test_plugin_rejects_like_reference(driver, tmp_path):

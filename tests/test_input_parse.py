@@ -1,0 +1,54 @@
+"""The library's input-file reader (pps_input_read) against the oracle's
+restatement of the reference's scan: the same format, side, extents and
+completed job for every fixture, and the same refusals.  CPU only (no
+device call)."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import pytest
+
+from helpers import args_to_spec
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def test_input_reader_matches_oracle(pps, ora):
+    cases = json.loads((GOLDEN / "input_cases.json").read_text())
+    for name, case in sorted(cases.items()):
+        spec = args_to_spec(case["args"])
+        path = GOLDEN / "inputs" / case["input"]
+        given = all(spec[f] for f in ("kmin", "kmax", "nmin", "nmax"))
+        if case["rc"] != 0:
+            with pytest.raises(pps.PPSError) as ei:
+                pps.InputFile(path, **spec)
+            assert ei.value.code == pps.PPS_ERR_SCANF
+            with pytest.raises(ora.OracleError):
+                ora.read_input(path, detect=not given)
+            continue
+        inp = pps.InputFile(path, **spec)
+        oi = ora.read_input(path, detect=not given)
+        info = inp.info()
+        assert info.records == len(oi.records), name
+        assert (info.k0, info.k1, info.n0, info.n1) == (oi.k0, oi.k1, oi.n0, oi.n1), name
+        assert {"newpgen": 1, "abcd": 2}[oi.format] == info.format and oi.sign == info.sign, name
+        ospec = ora.input_spec(oi, spec)
+        for f in ("kmin", "kmax", "nmin", "nmax", "sign"):
+            assert inp.spec[f] == ospec[f], (name, f)
+
+
+def test_input_reader_errors(pps, tmp_path):
+    with pytest.raises(pps.PPSError) as ei:
+        pps.InputFile(tmp_path / "missing.txt", pmin=10**12, pmax=10**12 + 10**6)
+    assert ei.value.code == pps.PPS_ERR_FOPEN
+    bad = tmp_path / "bad.txt"
+    bad.write_text("hello\n1 2\n")
+    with pytest.raises(pps.PPSError) as ei:
+        pps.InputFile(bad, pmin=10**12, pmax=10**12 + 10**6)
+    assert ei.value.code == pps.PPS_ERR_SCANF
+    one = tmp_path / "one_line.txt"
+    one.write_text("30:P:1:2:1\n")
+    with pytest.raises(pps.PPSError) as ei:
+        pps.InputFile(one, pmin=10**12, pmax=10**12 + 10**6)
+    assert ei.value.code == pps.PPS_ERR_SCANF
