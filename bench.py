@@ -55,6 +55,25 @@ def _dist():
     return ws, rank, local
 
 
+def shard_slices(total: int, ws: int, rank: int) -> list[int]:
+    """The p slices rank `rank` of `ws` walks: r, r+ws, r+2ws, ... (independent
+    units; no exchange between ranks in the data path)."""
+    return list(range(rank, total, ws))
+
+
+def reduce_over_ranks(x: float, op: str, ws: int, device: str) -> float:
+    """max or sum of a per-rank scalar (timing and counts only) through the
+    process group; the identity when ws == 1."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -293,7 +312,7 @@ def run_gpu(args) -> None:
         return ppsgpu.normalize(**dict(C2, pmin=lo, pmax=hi))
 
     total_slices = (C2["pmax"] - C2["pmin"] + SPAN - 1) // SPAN
-    my_slices = [s for s in range(total_slices) if s % ws == rank]
+    my_slices = shard_slices(total_slices, ws, rank)
     need = args.warmup + args.steps
     seq = [my_slices[i % len(my_slices)] for i in range(need)]
 
@@ -303,18 +322,10 @@ def run_gpu(args) -> None:
             torch.distributed.barrier()
 
     def max_over_ranks(x: float) -> float:
-        if ws == 1:
-            return x
-        t = torch.tensor([x], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_over_ranks(x, "max", ws, f"cuda:{local}")
 
     def sum_over_ranks(x: float) -> float:
-        if ws == 1:
-            return x
-        t = torch.tensor([x], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(t)
-        return float(t.item())
+        return reduce_over_ranks(x, "sum", ws, f"cuda:{local}")
 
     # ---- device-resident path (value)
     for i in range(args.warmup):
