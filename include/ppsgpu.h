@@ -292,6 +292,37 @@ int pps_job_wait(pps_server *s, uint64_t id, double timeout_s, pps_factor *out, 
                  size_t *nout, pps_job_result *res);
 int pps_server_get_stats(pps_server *s, pps_server_stats *st);
 
+/* ---- Checkpoints (main.c:304-372 write_checkpoint / read_checkpoint,
+   pps/app.c:1301-1352).  A job is done for every prime below p; count and sum
+   are the primes done and their wrapping sum, factor_count the factors found
+   so far (all with p below the boundary). */
+typedef struct {
+  uint64_t pmin;          /* the job's pmin */
+  uint64_t p;             /* boundary: every prime below p is done */
+  uint64_t count, sum;
+  uint32_t nmin, nmax;
+  uint32_t factor_count;
+  uint32_t pad;
+} pps_checkpoint;
+
+/* The reference's checkpoint file text, two lines:
+   "pmin=%llu,p=%llu,count=%llu,sum=0x%016llx,checksum=0x%016llx" (checksum =
+   pmin+p+count+sum) and "nmin=%u,nmax=%u,factor_count=%u".  Returns the length
+   written, or a negative code (PPS_ERR_OVERFLOW when cap is too small). */
+int pps_checkpoint_format(const pps_checkpoint *c, char *buf, size_t cap);
+/* Parses that text and validates it for job jp as the reference does: pmin
+   equal, pmin < p < pmax, the checksum, nmin and nmax equal.  An invalid
+   checkpoint is PPS_ERR_INVALID_PARAM (the reference ignores it and starts
+   over). */
+int pps_checkpoint_parse(const char *text, const pps_job_params *jp, pps_checkpoint *c);
+
+/* A served job's boundary: the p below which its pieces are walked (waves are
+   the unit, so the boundary is drained), with the factors found so far, sorted
+   (out == NULL: counts only).  A job resumed from it -- the same parameters
+   with pmin = c->p -- gives exactly the remaining factors. */
+int pps_job_checkpoint(pps_server *s, uint64_t id, pps_factor *out, size_t cap, size_t *nout,
+                       pps_checkpoint *c);
+
 /* Allocation-free walk (no counterpart in the reference): the walk and the
    output rule over np primes already in device memory (d_P), factors written
    to the caller's device buffer d_out (capacity out_cap, in no particular

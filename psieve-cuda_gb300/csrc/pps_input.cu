@@ -137,6 +137,41 @@ extern "C" int pps_input_get_info(const pps_input* in, pps_input_info* info) {
 
 extern "C" void pps_input_free(pps_input* in) { delete in; }
 
+// ---------------------------------------------------------------- checkpoints
+// main.c:304-326 write_checkpoint and pps/app.c:1348-1352 app_write_checkpoint.
+extern "C" int pps_checkpoint_format(const pps_checkpoint* c, char* buf, size_t cap) {
+  if (!c || (!buf && cap)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  const uint64_t checksum = c->pmin + c->p + c->count + c->sum;
+  const int n = snprintf(buf, cap,
+                         "pmin=%" PRIu64 ",p=%" PRIu64 ",count=%" PRIu64 ",sum=0x%016" PRIx64
+                         ",checksum=0x%016" PRIx64 "\nnmin=%u,nmax=%u,factor_count=%u\n",
+                         c->pmin, c->p, c->count, c->sum, checksum, c->nmin, c->nmax, c->factor_count);
+  if (n < 0) return set_err(PPS_ERR_INVALID_PARAM, "format");
+  if ((size_t)n >= cap) return set_err(PPS_ERR_OVERFLOW, "checkpoint text needs %d bytes", n + 1);
+  return n;
+}
+
+// main.c:332-372 read_checkpoint and pps/app.c:1301-1334 app_read_checkpoint
+// (the factors-file check of the latter is the caller's).
+extern "C" int pps_checkpoint_parse(const char* text, const pps_job_params* jp, pps_checkpoint* c) {
+  if (!text || !jp || !c) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
+  pps_checkpoint r;
+  memset(&r, 0, sizeof r);
+  uint64_t checksum = 0;
+  int used = 0;
+  if (sscanf(text, "pmin=%" SCNu64 ",p=%" SCNu64 ",count=%" SCNu64 ",sum=0x%" SCNx64 ",checksum=0x%" SCNx64 "\n%n",
+             &r.pmin, &r.p, &r.count, &r.sum, &checksum, &used) != 5 || used == 0)
+    return set_err(PPS_ERR_INVALID_PARAM, "invalid checkpoint: first line");
+  if (r.pmin != jp->pmin || r.p <= jp->pmin || r.p >= jp->pmax)
+    return set_err(PPS_ERR_INVALID_PARAM, "invalid checkpoint: p outside the job");
+  if (sscanf(text + used, "nmin=%u,nmax=%u,factor_count=%u", &r.nmin, &r.nmax, &r.factor_count) != 3)
+    return set_err(PPS_ERR_INVALID_PARAM, "invalid checkpoint: second line");
+  if (r.nmin != jp->nmin || r.nmax != jp->nmax) return set_err(PPS_ERR_INVALID_PARAM, "invalid checkpoint: n range");
+  if (r.pmin + r.p + r.count + r.sum != checksum) return set_err(PPS_ERR_INVALID_PARAM, "invalid checkpoint: checksum");
+  *c = r;
+  return PPS_OK;
+}
+
 // The reference's bitmap for one job as sorted bit numbers
 // (n - nmin) * width + kidx, width = (kmax - kmin) / kstep + 1.
 int input_keys_for_job(const pps_input* in, const pps_job_params* jp, std::vector<uint64_t>* keys,

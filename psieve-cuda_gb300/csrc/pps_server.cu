@@ -47,7 +47,8 @@ struct JobRec {
   uint64_t cursor = 0;   // next p handed to a wave
   uint64_t reserve = 0;  // bytes of the shared hit buffers reserved
   std::vector<pps_factor> factors;
-  uint64_t primes = 0, sum = 0;
+  uint64_t primes = 0, sum = 0;  // of the primes below done_p
+  uint64_t done_p = 0;           // boundary of the waves completed so far
   Clock::time_point t_submit, t_done;
 };
 
@@ -113,6 +114,7 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
   std::vector<JobRec*> failed;
   for (JobRec* j : admitted) {
     j->cursor = j->jp.pmin | 1ull;
+    j->done_p = j->jp.pmin;
     const int rc = batch_set_jobs(e, j->slot, &j->jp, 1);
     if (rc) {
       j->status = rc;
@@ -160,24 +162,45 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
       failed.push_back(j);
     }
     finishing.clear();
-  } else {
-    std::unordered_map<uint32_t, JobRec*> by_slot;
-    for (JobRec* j : in_wave) by_slot[j->slot] = j;
-    for (const pps_hit& h : surv) {
-      auto it = by_slot.find(batch_hit_slot(h));
-      if (it == by_slot.end()) continue;
-      it->second->factors.push_back(pps_factor{h.p, h.k, h.n, batch_hit_sign(h)});
+  }
+  // the jobs' prime counters after the wave (one copy of their slot range)
+  std::vector<uint64_t> pr, sm;
+  uint32_t slot_lo = 0;
+  if (!rc && !in_wave.empty()) {
+    uint32_t slot_hi = 0;
+    slot_lo = UINT32_MAX;
+    for (JobRec* j : in_wave) {
+      slot_lo = std::min(slot_lo, j->slot);
+      slot_hi = std::max(slot_hi, j->slot);
     }
-    for (JobRec* j : finishing) {
-      const int crc = batch_job_counts(e, j->slot, 1, &j->primes, &j->sum);
-      if (crc) {
+    pr.resize(slot_hi - slot_lo + 1);
+    sm.resize(slot_hi - slot_lo + 1);
+    if (int crc = batch_job_counts(e, slot_lo, pr.size(), pr.data(), sm.data())) {
+      for (JobRec* j : in_wave) {
         j->status = crc;
         failed.push_back(j);
       }
+      finishing.clear();
     }
   }
   {
     std::lock_guard<std::mutex> lk(s->mu);
+    if (!rc && !pr.empty()) {
+      // survivors to their jobs, and each job's drained boundary (its checkpoint)
+      std::unordered_map<uint32_t, JobRec*> by_slot;
+      for (JobRec* j : in_wave) by_slot[j->slot] = j;
+      for (const pps_hit& h : surv) {
+        auto it = by_slot.find(batch_hit_slot(h));
+        if (it == by_slot.end()) continue;
+        it->second->factors.push_back(pps_factor{h.p, h.k, h.n, batch_hit_sign(h)});
+      }
+      for (JobRec* j : in_wave) {
+        if (j->status) continue;
+        j->primes = pr[j->slot - slot_lo];
+        j->sum = sm[j->slot - slot_lo];
+        j->done_p = std::min(j->cursor, j->jp.pmax);
+      }
+    }
     if (!pieces.empty()) {
       s->st.waves++;
       s->st.busy_ms += busy;
@@ -331,6 +354,32 @@ extern "C" int pps_job_wait(pps_server* s, uint64_t id, double timeout_s, pps_fa
   const int status = j->status;
   s->jobs.erase(it);
   if (status) return set_err(status, "job %llu failed", (unsigned long long)id);
+  return PPS_OK;
+}
+
+extern "C" int pps_job_checkpoint(pps_server* s, uint64_t id, pps_factor* out, size_t cap, size_t* nout,
+                                  pps_checkpoint* c) {
+  if (!s) return set_err(PPS_ERR_INVALID_PARAM, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return set_err(PPS_ERR_NOT_FOUND, "no job %llu", (unsigned long long)id);
+  const JobRec* j = it->second.get();
+  const size_t nf = j->factors.size();
+  if (nout) *nout = nf;
+  if (c) {
+    memset(c, 0, sizeof *c);
+    c->pmin = j->jp.pmin;
+    c->p = j->state == PPS_JOB_QUEUED ? j->jp.pmin : j->done_p;
+    c->count = j->primes;
+    c->sum = j->sum;
+    c->nmin = j->jp.nmin;
+    c->nmax = j->jp.nmax;
+    c->factor_count = (uint32_t)nf;
+  }
+  if (out) {
+    if (nf > cap) return set_err(PPS_ERR_OVERFLOW, "%zu factors, buffer holds %zu", nf, cap);
+    if (nf) memcpy(out, j->factors.data(), nf * sizeof(pps_factor));
+  }
   return PPS_OK;
 }
 

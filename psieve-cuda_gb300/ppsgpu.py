@@ -115,6 +115,29 @@ PPS_ERR_FOPEN = -108
 PPS_ERR_SCANF = -140
 
 
+class Checkpoint(ctypes.Structure):
+    _fields_ = [("pmin", ctypes.c_uint64), ("p", ctypes.c_uint64), ("count", ctypes.c_uint64),
+                ("sum", ctypes.c_uint64), ("nmin", ctypes.c_uint32), ("nmax", ctypes.c_uint32),
+                ("factor_count", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
+def checkpoint_format(c: Checkpoint, lib=None) -> str:
+    """The reference's checkpoint file text (main.c:304-326, pps/app.c:1348-1352)."""
+    lib = lib or load()
+    buf = ctypes.create_string_buffer(512)
+    n = lib.pps_checkpoint_format(ctypes.byref(c), buf, len(buf))
+    if n < 0:
+        _check(lib, n)
+    return buf.value.decode()
+
+
+def checkpoint_parse(text: str, jp: "JobParams", lib=None) -> Checkpoint:
+    lib = lib or load()
+    c = Checkpoint()
+    _check(lib, lib.pps_checkpoint_parse(text.encode(), ctypes.byref(jp), ctypes.byref(c)))
+    return c
+
+
 class InputInfo(ctypes.Structure):
     _fields_ = [("format", ctypes.c_int32), ("sign", ctypes.c_int32),
                 ("records", ctypes.c_uint64), ("k0", ctypes.c_uint64), ("k1", ctypes.c_uint64),
@@ -213,6 +236,10 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_input_get_info": (ctypes.c_int, [ctypes.c_void_p, P(InputInfo)]),
         "pps_input_free": (None, [ctypes.c_void_p]),
         "pps_engine_set_input": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+        "pps_checkpoint_format": (ctypes.c_int, [P(Checkpoint), ctypes.c_char_p, ctypes.c_size_t]),
+        "pps_checkpoint_parse": (ctypes.c_int, [ctypes.c_char_p, P(JobParams), P(Checkpoint)]),
+        "pps_job_checkpoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                              ctypes.c_size_t, szp, P(Checkpoint)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -485,3 +512,18 @@ class Server:
         st = ServerStats()
         _check(self.lib, self.lib.pps_server_get_stats(self.h, ctypes.byref(st)))
         return st
+
+    def checkpoint(self, jid: int) -> tuple[np.ndarray, Checkpoint]:
+        """A running job's drained boundary and the factors found below it."""
+        c = Checkpoint()
+        n = ctypes.c_size_t()
+        while True:
+            _check(self.lib, self.lib.pps_job_checkpoint(self.h, jid, None, 0, ctypes.byref(n),
+                                                         ctypes.byref(c)))
+            out = np.zeros(max(n.value, 1) + 64, dtype=FACTOR_DTYPE)
+            rc = self.lib.pps_job_checkpoint(self.h, jid, out.ctypes.data_as(ctypes.c_void_p), out.size,
+                                             ctypes.byref(n), ctypes.byref(c))
+            if rc == PPS_ERR_OVERFLOW:
+                continue  # more factors arrived between the two calls
+            _check(self.lib, rc)
+            return out[: n.value], c

@@ -82,3 +82,35 @@ def test_server_wait_timeout_poll_and_unknown(pps):
         with pytest.raises(pps.PPSError) as ei:
             srv.submit(pps.JobParams())  # not normalised
         assert ei.value.code == pps.PPS_ERR_INVALID_PARAM
+
+
+def test_server_checkpoint_resumes_exactly(pps, engine):
+    """A job's checkpoint mid-run (small waves: the boundary moves wave by wave):
+    the factors below the boundary plus a job resumed at the boundary give the
+    whole result, and the prime fingerprints add up."""
+    import time
+
+    jp = pps.normalize(pmin=10**12, pmax=10**12 + 3 * 10**9, kmin=1201, kmax=9999, nmin=2000,
+                       nmax=60000)
+    with pps.Server(0, wave_segments=256) as srv:
+        jid = srv.submit(jp)
+        ck = None
+        for _ in range(2000):
+            fac, c = srv.checkpoint(jid)
+            if jp.pmin < c.p < jp.pmax:
+                ck = (fac, c)
+                break
+            time.sleep(0.002)
+        full, res = srv.wait(jid)
+    assert ck is not None, "no boundary seen while the job ran"
+    part, c = ck
+    whole = pps.factors_to_tuples(full)
+    assert pps.factors_to_tuples(part) == [f for f in whole if f[0] < c.p]
+    assert c.factor_count == len(part)
+    rest = pps.JobParams(**dict(jp.as_dict(), pmin=c.p))
+    tail, tst = engine.run_job(rest)
+    assert pps.factors_to_tuples(tail) == [f for f in whole if f[0] >= c.p]
+    assert c.count + tst.primes == res.primes
+    assert (c.sum + tst.prime_sum) % 2**64 == res.prime_sum
+    text = pps.checkpoint_format(c)
+    assert pps.checkpoint_parse(text, jp).p == c.p
