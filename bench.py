@@ -444,6 +444,23 @@ def run_profile(args) -> None:
     eng.close()
 
 
+def run_profile_batched(args) -> None:
+    """The configuration-4 workload through pps_run_batch only (a warm-up batch
+    of 64 jobs, then the 512 jobs once), for launch lists and captures of the
+    batched kernels."""
+    import ppsgpu
+
+    eng = ppsgpu.Engine(0)
+    jobs, _ = ppsgpu.mixed_jobs(seed=1, count=args.mixed_jobs)
+    eng.run_batch(jobs[:64])
+    t0 = time.perf_counter()
+    _, st = eng.run_batch(jobs)
+    dt = time.perf_counter() - t0
+    print(f"batched: {len(jobs)} jobs, {st.primes} primes, {st.steps} steps, {st.waves} waves, "
+          f"{dt:.3f} s, {st.steps / dt:.4e} steps/s", flush=True)
+    eng.close()
+
+
 def run_sweep(args) -> None:
     """Walk rate of every kernel variant on the first slice (stderr report)."""
     import ppsgpu
@@ -487,11 +504,14 @@ def main() -> None:
     ap.add_argument("--profile-reps", type=int, default=1)
     ap.add_argument("--variant", type=int, default=5)
     ap.add_argument("--sweep", action="store_true")
+    ap.add_argument("--profile-batched", action="store_true")
     ap.add_argument("--sweep-span", type=int, default=1 << 28)
     ap.add_argument("--sweep-nwidth", type=int, default=100000)
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
+    elif args.profile_batched:
+        run_profile_batched(args)
     elif args.sweep:
         run_sweep(args)
     elif args.impl == "reference":
