@@ -210,6 +210,30 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
             "batched_n_steps_per_s": bst.steps / t_batch}
 
 
+def run_other_configs(eng) -> dict:
+    """Configurations 1 (in full) and 3 (one 2^31-wide slice) through pps_run_job,
+    timed after one warm-up run each (walk tuning per step class)."""
+    import ppsgpu
+
+    out = {}
+    cases = {
+        "config1_full": dict(pmin=10**12, pmax=10**12 + 2 * 10**8, kmin=1201, kmax=9999, nmin=2000,
+                             nmax=3000),
+        "config3_slice": dict(pmin=(1 << 62) - (1 << 34), pmax=(1 << 62) - (1 << 34) + SPAN, kmin=3,
+                              kmax=9999, nmin=100000, nmax=1000000, sign=-1),
+    }
+    for name, spec in cases.items():
+        jp = ppsgpu.normalize(**spec)
+        eng.run_job(jp)
+        t0 = time.perf_counter()
+        fac, st = eng.run_job(jp)
+        dt = time.perf_counter() - t0
+        out[name] = {"primes": int(st.primes), "seconds": dt, "primes_per_s": st.primes / dt,
+                     "n_steps_per_s": st.steps / dt, "factors": len(fac), "nstep": int(jp.nstep),
+                     "walk_step": int(jp.step), "variant": int(st.variant)}
+    return out
+
+
 def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -> dict:
     """Configuration 5: Poisson arrivals at each rate for `window` seconds of
     jobs from the configuration-4 distribution, submitted to the serving loop
@@ -409,6 +433,7 @@ def run_gpu(args) -> None:
     cpu = None if args.no_cpu else cpu_sample(args.ref_seconds)
     batched = None if args.no_batched else run_mixed(eng, args.mixed_jobs)
     serving = None if args.no_serving else run_serving(window=args.serve_window)
+    others = None if args.no_batched else run_other_configs(eng)
     line = {"metric": METRIC, "value": value, "unit": "primes/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -422,7 +447,7 @@ def run_gpu(args) -> None:
                          "filter": sum(s.filter_ms for s in stats)},
             "factors": sum(s.factors for s in stats),
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "batched": batched, "serving": serving}
+            "batched": batched, "serving": serving, "other_configs": others}
     print(json.dumps(line), flush=True)
     eng.close()
     if ws > 1:
