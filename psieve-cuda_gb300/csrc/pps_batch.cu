@@ -45,7 +45,8 @@ struct BJob {
   uint32_t chunk;  // primes per work chunk: about the same walk steps for every job
   // win_sh < 32: the small-p window, K < 2^win_sh or the low bits in win_mask
   // all zero; 32: K < (win_hi + 1) * 2^32 or the low bits in win_mask zero
-  uint32_t win_sh, pad;
+  uint32_t win_sh;
+  uint32_t shift_ok;  // step < 32 and pmax <= 2^(32+step): walk form 1
 };
 
 struct BBatch {
@@ -449,29 +450,50 @@ __device__ __forceinline__ void b_record(uint32_t klo, uint32_t khi, uint32_t n,
   }
 }
 
-template <bool S32>
-__device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi, uint32_t pinv_s,
+// Walk-step forms of the batched walk:
+//   0  s == 32: the carry-chain REDC by 2^32;
+//   1  s < 32 and p <= 2^(32+s): K' = K * 2^(32-s) (< 2^64) through the same
+//      chain, since (K + m p) / 2^s == (K' + m' p) / 2^32 with
+//      m' = lo32(K') * (-p^-1) mod 2^32 = m * 2^(32-s);
+//   2  s < 32, larger p: the shift-REDC with a wide multiply-add.
+// pinv is lo32(-p^-1) for forms 0 and 1 and that << (32-s) for form 2.
+template <int FORM>
+__device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi, uint32_t pinv,
                                        uint32_t s) {
-  if (S32) step_chain32(klo, khi, plo, phi, pinv_s);
-  else step_form0<false>(klo, khi, plo, phi, pinv_s, s);
+  if (FORM == 0) {
+    step_chain32(klo, khi, plo, phi, pinv);
+  } else if (FORM == 1) {
+    const uint32_t sh = 32u - s;
+    uint32_t lo = klo << sh, hi = __funnelshift_l(klo, khi, sh);
+    step_chain32(lo, hi, plo, phi, pinv);
+    klo = lo;
+    khi = hi;
+  } else {
+    step_form0<false>(klo, khi, plo, phi, pinv, s);
+  }
+}
+
+template <int FORM>
+__device__ __forceinline__ uint32_t b_pinv(uint64_t ps, uint32_t s) {
+  return FORM == 2 ? (lo32(ps) << (32u - s)) : lo32(ps);
 }
 
 // One round: every lane walks one prime of the same job; flagged blocks of U
 // steps (and the partial last block) go to the warp's queue and are re-checked
 // exactly once the round's walks are done.  A twin job (TW) walks K = 2^-n, the
 // -1 side's value, and tests p - K, the +1 side's, at the same step.
-template <bool S32, int U, bool WSH, bool TW>
+template <int FORM, int U, bool WSH, bool TW>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
                                         uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
                                         uint32_t* hit_count, uint32_t hit_cap) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t s = S32 ? 32u : J.step;
+  const uint32_t s = FORM == 0 ? 32u : J.step;
   const uint32_t nsteps = J.nsteps, full = nsteps / (uint32_t)U;
   const uint32_t tag = job | (J.proth == 1u ? SIDE_PROTH : 0u);  // the walked value's side
   qp[lane] = p;
   if (valid) {
     const uint32_t plo = lo32(p), phi = hi32(p);
-    const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
+    const uint32_t pinv_s = b_pinv<FORM>(ps, s);
     const uint64_t x = inv_pow2(J.nmin, p, ps);
     const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
@@ -497,7 +519,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
         else
           f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
         if (TW) f |= (mk64(klo, khi) > tw_above) | ((klo & win_mask) == tw_low);
-        b_step<S32>(klo, khi, plo, phi, pinv_s, s);
+        b_step<FORM>(klo, khi, plo, phi, pinv_s, s);
       }
       if (f) {
         const uint32_t pos = atomicAdd(qc, 1u);
@@ -531,7 +553,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
       }
       uint32_t klo = lo32(K), khi = hi32(K);
       const uint32_t oplo = lo32(op), ophi = hi32(op);
-      const uint32_t opinv = S32 ? lo32(ops) : (lo32(ops) << (32u - s));
+      const uint32_t opinv = b_pinv<FORM>(ops, s);
 #pragma unroll 1
       for (uint32_t u = 0; u < nblk; ++u) {
         b_record(klo, khi, n0 + s * u, s, op, tag, J, hits, hit_count, hit_cap);
@@ -539,12 +561,12 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
           const uint64_t v = op - mk64(klo, khi);
           b_record(lo32(v), hi32(v), n0 + s * u, s, op, job | SIDE_PROTH, J, hits, hit_count, hit_cap);
         }
-        b_step<S32>(klo, khi, oplo, ophi, opinv, s);
+        b_step<FORM>(klo, khi, oplo, ophi, opinv, s);
       }
     }
   } else if (valid) {
     const uint32_t plo = lo32(p), phi = hi32(p);
-    const uint32_t pinv_s = S32 ? lo32(ps) : (lo32(ps) << (32u - s));
+    const uint32_t pinv_s = b_pinv<FORM>(ps, s);
     const uint64_t x = inv_pow2(J.nmin, p, ps);
     const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
@@ -555,7 +577,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
         const uint64_t v = p - mk64(klo, khi);
         b_record(lo32(v), hi32(v), J.nmin + s * t, s, p, job | SIDE_PROTH, J, hits, hit_count, hit_cap);
       }
-      b_step<S32>(klo, khi, plo, phi, pinv_s, s);
+      b_step<FORM>(klo, khi, plo, phi, pinv_s, s);
     }
   }
   __syncwarp();
@@ -595,23 +617,22 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
       const bool valid = r + lane < count;
       const uint64_t pi = first + r + (valid ? lane : 0u);
       const uint64_t p = P[pi], ps = Pinv[pi];
-#define PPS_BROUND(S32_, WSH_, TW_)                                                                     \
-  b_round<S32_, U, WSH_, TW_>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, \
-                              hit_count, hit_cap)
+#define PPS_BROUND(FORM_, WSH_, TW_)                                                                    \
+  b_round<FORM_, U, WSH_, TW_>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, \
+                               hit_count, hit_cap)
+#define PPS_BROUND_F(FORM_)                                                                             \
+  do {                                                                                                  \
+    if (wsh) {                                                                                          \
+      if (tw) PPS_BROUND(FORM_, true, true); else PPS_BROUND(FORM_, true, false);                       \
+    } else {                                                                                            \
+      if (tw) PPS_BROUND(FORM_, false, true); else PPS_BROUND(FORM_, false, false);                     \
+    }                                                                                                   \
+  } while (0)
       const bool wsh = J.win_sh < 32u, tw = J.proth == 2u;
-      if (J.step == 32) {
-        if (wsh) {
-          if (tw) PPS_BROUND(true, true, true); else PPS_BROUND(true, true, false);
-        } else {
-          if (tw) PPS_BROUND(true, false, true); else PPS_BROUND(true, false, false);
-        }
-      } else {
-        if (wsh) {
-          if (tw) PPS_BROUND(false, true, true); else PPS_BROUND(false, true, false);
-        } else {
-          if (tw) PPS_BROUND(false, false, true); else PPS_BROUND(false, false, false);
-        }
-      }
+      if (J.step == 32) PPS_BROUND_F(0);
+      else if (J.shift_ok) PPS_BROUND_F(1);
+      else PPS_BROUND_F(2);
+#undef PPS_BROUND_F
 #undef PPS_BROUND
     }
   }
@@ -776,6 +797,8 @@ BJob make_job(const pps_job_params& jp) {
   J.sign = jp.sign;
   J.chunk = 32;
   small_p_window(jp, &J);
+  // form 1 keeps K * 2^(32-step) below 2^64: every K < p <= pmax <= 2^(32+step)
+  J.shift_ok = jp.step < 32 && (jp.pmax - 1) >> (32 + jp.step) == 0 ? 1u : 0u;
   return J;
 }
 
