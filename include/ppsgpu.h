@@ -134,7 +134,7 @@ int pps_engine_sm_count(const pps_engine *e);
 int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 
 /* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
-#define PPS_NUM_VARIANTS 18
+#define PPS_NUM_VARIANTS 22
 int pps_engine_set_variant(pps_engine *e, int variant);
 
 /* Whole job: device sieve of [pmin,pmax), walk, filter.  Factors are sorted by

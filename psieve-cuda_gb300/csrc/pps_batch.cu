@@ -764,17 +764,10 @@ int floor_lg2(uint64_t x) { return 63 - __builtin_clzll(x | 1ull); }
 // against P(low t+1-kb bits zero) = 2^-(t+1-kb).  It stays exact while
 // K < p <= 2^(t+32), so that the funnel shift sees all of K >> t.
 void small_p_window(const pps_job_params& jp, BJob* J) {
-  J->win_sh = 32;
-  const int kb = floor_lg2(jp.kmax) + 1;
-  const int lp = floor_lg2(jp.pmin);
-  if (lp + kb - 64 >= 0) return;
-  const int B = floor_lg2(jp.pmax - 1) + 1;  // every p, and so every K, is below 2^B
-  int t = (lp + kb - 1) / 2;
-  t = std::max(t, B - 32);
-  t = std::max(t, kb);
-  if (t >= 32) return;
-  J->win_sh = (uint32_t)t;
-  J->win_mask = (1u << (t + 1 - kb)) - 1u;
+  uint32_t t, mask;
+  small_p_window_of(&jp, &t, &mask);
+  J->win_sh = t;
+  if (t < 32) J->win_mask = mask;
 }
 
 BJob make_job(const pps_job_params& jp) {

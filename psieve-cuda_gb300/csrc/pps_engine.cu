@@ -360,6 +360,24 @@ extern "C" int pps_sieve_range(pps_engine* e, uint64_t lo, uint64_t hi, uint32_t
 }
 
 // ------------------------------------------------------------------- walk
+// t = (lg p + kb - 1) / 2 balances P(K < 2^t) ~ 2^(t - lg p) against
+// P(low t+1-kb bits zero) = 2^-(t+1-kb) (kmax < 2^kb); it stays exact while
+// K < p <= 2^(t+32), so that a funnel shift sees all of K >> t.
+void pps::small_p_window_of(const pps_job_params* jp, uint32_t* t_out, uint32_t* mask_out) {
+  *t_out = 32;
+  *mask_out = 0;
+  const int kb = lg2u64(jp->kmax) + 1;
+  const int lp = lg2u64(jp->pmin);
+  if (lp + kb - 64 >= 0) return;
+  const int B = lg2u64(jp->pmax - 1) + 1;  // every p, and so every K, is below 2^B
+  int t = (lp + kb - 1) / 2;
+  t = std::max(t, B - 32);
+  t = std::max(t, kb);
+  if (t >= 32) return;
+  *t_out = (uint32_t)t;
+  *mask_out = (1u << (t + 1 - kb)) - 1u;
+}
+
 static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
   memset(a, 0, sizeof *a);
   a->kmin = jp->kmin;
@@ -382,11 +400,20 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
   a->win_mask = t >= 32 ? 0xffffffffu : ((1u << t) - 1u);
   a->kmax32 = jp->kmax < (1ull << 32) ? (uint32_t)jp->kmax : 0xffffffffu;
   a->bound_hi = jp->kmax < (1ull << 32) ? (uint32_t)(jp->kmax >> 1) : 0xffffffffu;
+  pps::small_p_window_of(jp, &a->sh_t, &a->sh_mask);
+  a->shift_ok = jp->step < 32 && ((jp->pmax - 1) >> (32 + jp->step)) == 0 ? 1u : 0u;
 }
 
 static int variant_ok(const pps_job_params* jp, int v) {
   if ((v == 7 || v == 8) && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
-  if (v >= 10 && jp->step != 32) return 0;                       // lean kernels: 32-bit steps
+  if (v >= 10 && v <= 18 && jp->step != 32) return 0;            // queued kernels: 32-bit steps
+  if (v >= 18) {
+    WalkArgs a;
+    fill_walk_args(jp, &a);
+    if (v == 19 && (!a.shift_ok || a.win_hi != 0)) return 0;       // shifted chain, u == 0 window
+    if (v >= 20 && !a.shift_ok) return 0;                          // shifted chain
+    if ((v == 18 || v >= 20) && a.sh_t >= 32) return 0;            // small-p window
+  }
   if (v == 10 || v == 13 || v == 15) {                            // running-minimum window: u == 0
     WalkArgs a;
     fill_walk_args(jp, &a);

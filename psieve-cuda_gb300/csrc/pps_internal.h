@@ -53,6 +53,8 @@ struct WalkArgs {
   uint32_t win_mask;        // ... or (lo word & win_mask) == 0
   uint32_t kmax32;          // low-bit pre-test (kmax < 2^32)
   uint32_t bound_hi;        // single-bound pre-test: hi word <= bound_hi
+  uint32_t sh_t, sh_mask;   // small-p window: K < 2^sh_t or (lo & sh_mask) == 0; sh_t 32: none
+  uint32_t shift_ok;        // step < 32 and pmax <= 2^(32+step): the shifted chain step
   uint32_t idx_base;        // added to the prime index in hit records
   pps_hit* hits;
   uint32_t* hit_count;      // may exceed hit_cap: overflow is detected by host
@@ -64,6 +66,10 @@ const char* walk_variant_name(int v);
 // Pre-test constants of a normalised job, and whether variant v is exact for it
 // (defined in pps_engine.cu).
 void walk_args_for_job(const pps_job_params* jp, WalkArgs* a);
+// The small-p window of a job: where p is far below 2^(64 - bits(kmax)) the
+// hi-word window passes most steps; there K < 2^t or the low t+1-bits(kmax)
+// bits zero is tested instead (*t = 32: not used).
+void small_p_window_of(const pps_job_params* jp, uint32_t* t, uint32_t* mask);
 int walk_variant_exact(const pps_job_params* jp, int v);
 // Record an error message for pps_last_error(); returns code.
 int set_error_text(int code, const char* msg);

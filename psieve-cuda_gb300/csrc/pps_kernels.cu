@@ -365,10 +365,10 @@ constexpr int WQ_WARPS = 8;   // warps per 256-thread block
 
 __device__ __forceinline__ void record_exact(uint32_t klo, uint32_t khi, uint32_t n, uint64_t p, uint32_t idx,
                                              uint64_t kmin, uint64_t kmax, uint32_t nmax, pps_hit* hits,
-                                             uint32_t* hit_count, uint32_t hit_cap) {
+                                             uint32_t* hit_count, uint32_t hit_cap, uint32_t step = 32u) {
   const uint32_t i = klo ? (uint32_t)(__ffs(klo) - 1) : (uint32_t)(31 + __ffs(khi));
   const uint64_t k = mk64(klo, khi) >> (i & 63u);
-  const bool hit = (i < 32u) && (k <= kmax) && (k >= kmin) && (n + i < nmax);
+  const bool hit = (i < step) && (k <= kmax) && (k >= kmin) && (n + i < nmax);
   const unsigned act = __activemask();
   const unsigned hm = __ballot_sync(act, hit);
   if (hm) {
@@ -391,14 +391,34 @@ __device__ __forceinline__ void record_exact(uint32_t klo, uint32_t khi, uint32_
   }
 }
 
-template <int TEST, int U, int MINB>
+// The queued walk step: FORM 0 is the chain REDC by 2^32 (s = 32); FORM 1 walks
+// s < 32 through the same chain on K * 2^(32-s), exact while p <= 2^(32+s)
+// ((K + m p) / 2^s == (K 2^(32-s) + m 2^(32-s) p) / 2^32).
+template <int FORM>
+__device__ __forceinline__ void q_step(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi, uint32_t pinv,
+                                       uint32_t sh) {
+  if (FORM == 0) {
+    step_chain32(klo, khi, plo, phi, pinv);
+  } else {
+    uint32_t lo = klo << sh, hi = __funnelshift_l(klo, khi, sh);
+    step_chain32(lo, hi, plo, phi, pinv);
+    klo = lo;
+    khi = hi;
+  }
+}
+
+// SH: the small-p window (K < 2^sh_t or the low bits in sh_mask zero) in place
+// of the hi-word window, for p far below 2^(64 - bits(kmax)).
+template <int TEST, int U, int MINB, int FORM = 0, bool SH = false>
 __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
   __shared__ uint32_t q_ent[WQ_WARPS][WQ_CAP];
   __shared__ uint64_t q_p[WQ_WARPS][32];
   __shared__ uint64_t q_k[WQ_WARPS][32];  // start value of each lane's partial last block
   __shared__ uint32_t q_cnt[WQ_WARPS];
   const uint64_t np = a.d_np ? *a.d_np : a.np;
-  const uint32_t win_hi = a.win_hi, win_mask = a.win_mask, bound_hi = a.bound_hi;
+  const uint32_t win_hi = a.win_hi, win_mask = SH ? a.sh_mask : a.win_mask, bound_hi = a.bound_hi;
+  const uint32_t sh_t = a.sh_t;
+  const uint32_t s = FORM == 0 ? 32u : a.step, sh = 32u - s;
   const uint32_t nsteps = a.nsteps, nmin = a.nmin;
   const uint32_t full = nsteps / (uint32_t)U;  // whole blocks of U steps
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
@@ -422,10 +442,10 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         bool f = false;
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          if (TEST == 0) acc = min(acc, min(khi, klo & win_mask));
+          if (TEST == 0) acc = min(acc, min(SH ? __funnelshift_rc(klo, khi, sh_t) : khi, klo & win_mask));
           else if (TEST == 1) f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
           else f |= khi <= bound_hi;
-          step_chain32(klo, khi, plo, phi, pinv);
+          q_step<FORM>(klo, khi, plo, phi, pinv, sh);
         }
         if (TEST == 0) f = acc == 0u;
         if (f) {
@@ -452,7 +472,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         const uint64_t ops = neg_inv64(op);
         const uint32_t t0 = (uint32_t)U * blk;
         const uint32_t nblk = min((uint32_t)U, nsteps - t0);
-        const uint32_t n0 = nmin + 32u * t0;
+        const uint32_t n0 = nmin + s * t0;
         uint64_t K;
         if (blk == full) {
           K = q_k[wib][owner];
@@ -464,9 +484,9 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         const uint32_t oplo = lo32(op), ophi = hi32(op), opinv = lo32(ops);
 #pragma unroll 1
         for (uint32_t u = 0; u < nblk; ++u) {
-          record_exact(klo, khi, n0 + 32u * u, op, a.idx_base + (uint32_t)(base + owner), a.kmin, a.kmax,
-                       a.nmax, a.hits, a.hit_count, a.hit_cap);
-          step_chain32(klo, khi, oplo, ophi, opinv);
+          record_exact(klo, khi, n0 + s * u, op, a.idx_base + (uint32_t)(base + owner), a.kmin, a.kmax,
+                       a.nmax, a.hits, a.hit_count, a.hit_cap, s);
+          q_step<FORM>(klo, khi, oplo, ophi, opinv, sh);
         }
       }
     } else if (valid) {
@@ -479,9 +499,9 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
       const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
 #pragma unroll 1
       for (uint32_t t = 0; t < nsteps; ++t) {
-        record_exact(klo, khi, nmin + 32u * t, p, a.idx_base + (uint32_t)pi, a.kmin, a.kmax, a.nmax,
-                     a.hits, a.hit_count, a.hit_cap);
-        step_chain32(klo, khi, plo, phi, pinv);
+        record_exact(klo, khi, nmin + s * t, p, a.idx_base + (uint32_t)pi, a.kmin, a.kmax, a.nmax,
+                     a.hits, a.hit_count, a.hit_cap, s);
+        q_step<FORM>(klo, khi, plo, phi, pinv, sh);
       }
     }
     __syncwarp();
@@ -499,7 +519,8 @@ static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
     {"form2-window-u8-block-ilp2"}, {"chain-lowbit-u8-block"}, {"form0-lowbit-u8-block"},
     {"chain-window-u16-block"}, {"queue-min-u8"}, {"queue-window-u8"}, {"queue-bound-u8"},
     {"queue-min-u16"}, {"queue-bound-u16"}, {"queue-min-u8-r40"}, {"queue-bound-u8-r40"},
-    {"queue-window-u8-r40"},
+    {"queue-window-u8-r40"}, {"queue-smallp-u8"}, {"queue-shift-min-u8"}, {"queue-shift-smallp-u8"},
+    {"queue-shift-smallp-u16"},
 };
 
 const char* walk_variant_name(int v) {
@@ -529,6 +550,10 @@ static walk_fn pick(int v) {
     case 15: return S32 ? k_walk32q<0, 8, 6> : nullptr;
     case 16: return S32 ? k_walk32q<2, 8, 6> : nullptr;
     case 17: return S32 ? k_walk32q<1, 8, 6> : nullptr;
+    case 18: return S32 ? k_walk32q<0, 8, 8, 0, true> : nullptr;
+    case 19: return S32 ? nullptr : k_walk32q<0, 8, 8, 1, false>;
+    case 20: return S32 ? nullptr : k_walk32q<0, 8, 8, 1, true>;
+    case 21: return S32 ? nullptr : k_walk32q<0, 16, 8, 1, true>;
   }
   return nullptr;
 }

@@ -63,14 +63,18 @@ def test_every_walk_variant_matches_oracle(pps, engine, ora, variant):
              nmin=100000, nmax=140000, sign=-1),
     ]
     engine.set_variant(variant)
+    ran = 0
     try:
         for spec in specs:
             got, st = _gpu_lines(pps, engine, spec)
             want, cnt, _ = ora.run(ora.normalize(**spec))
             assert got == lines_of(ora.tuples(want)), (variant, spec)
             assert st.primes == cnt
+            ran += st.variant == variant
     finally:
         engine.set_variant(-1)
+    # every variant is exact for at least one of the jobs, so it really ran
+    assert ran >= 1, variant
 
 
 def test_sieve_matches_oracle(engine, ora):
