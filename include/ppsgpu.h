@@ -49,10 +49,12 @@ extern "C" {
 /* sign of a twin job: both k*2^n+1 and k*2^n-1 from one walk, as the
    reference's twin build (tpsieve, -DSEARCH_TWIN: pps/app.c:1071-1107,
    pps/appcu.cu:177-180, 741-767) reports them; k == 3 (mod 6) unless -M/-s
-   say otherwise.  Each factor carries its own c.  Twin jobs run on the
-   batched walk: pps_run_job, pps_run_batch and the serving loop take them;
-   the host-prime entry points and the appcu.h layer return
-   PPS_ERR_NOT_IMPLEMENTED. */
+   say otherwise.  Each factor carries its own c.  pps_run_job, pps_run_batch
+   and the serving loop run twin jobs on the batched walk; pps_check_primes*
+   on the one-job twin kernels (which need s = 32, or p <= 2^(32+s):
+   PPS_ERR_NOT_IMPLEMENTED otherwise; raw candidates of a twin job carry their
+   side in idx bit 31).  The appcu.h layer and pps_check_primes_noalloc take
+   one side only. */
 #define PPS_SIGN_TWIN 2
 
 /* A job as the user states it; zero means "not given" exactly as in the
@@ -134,7 +136,7 @@ int pps_engine_sm_count(const pps_engine *e);
 int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 
 /* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
-#define PPS_NUM_VARIANTS 22
+#define PPS_NUM_VARIANTS 26
 int pps_engine_set_variant(pps_engine *e, int variant);
 
 /* Whole job: device sieve of [pmin,pmax), walk, filter.  Factors are sorted by

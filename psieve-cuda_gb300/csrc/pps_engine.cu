@@ -405,14 +405,19 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
 }
 
 static int variant_ok(const pps_job_params* jp, int v) {
+  // variants 22-25 walk both sides of a twin job; every other variant one side
+  const bool twin = jp->sign == PPS_SIGN_TWIN;
+  if (twin != (v >= 22)) return 0;
   if ((v == 7 || v == 8) && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
-  if (v >= 10 && v <= 18 && jp->step != 32) return 0;            // queued kernels: 32-bit steps
+  if (((v >= 10 && v <= 18) || v == 22 || v == 23) && jp->step != 32) return 0;  // 32-bit steps
   if (v >= 18) {
     WalkArgs a;
     fill_walk_args(jp, &a);
-    if (v == 19 && (!a.shift_ok || a.win_hi != 0)) return 0;       // shifted chain, u == 0 window
-    if (v >= 20 && !a.shift_ok) return 0;                          // shifted chain
-    if ((v == 18 || v >= 20) && a.sh_t >= 32) return 0;            // small-p window
+    const bool shifted = (v >= 19 && v <= 21) || v >= 24, smallp = v == 18 || v == 20 || v == 21 ||
+                                                                    v == 23 || v == 25;
+    if (v == 19 && a.win_hi != 0) return 0;  // running minimum: u == 0 window
+    if (shifted && !a.shift_ok) return 0;    // shifted chain: s < 32, p <= 2^(32+s)
+    if (smallp && a.sh_t >= 32) return 0;    // small-p window
   }
   if (v == 10 || v == 13 || v == 15) {                            // running-minimum window: u == 0
     WalkArgs a;
@@ -459,7 +464,7 @@ int set_error_text(int code, const char* msg) { return set_err(code, "%s", msg);
 // range and keep the fastest for this step class.
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
                     uint64_t np) {
-  const int cls = jp->step == 32 ? 1 : 0;
+  const int cls = (jp->step == 32 ? 1 : 0) + (jp->sign == PPS_SIGN_TWIN ? 2 : 0);
   // a forced variant is honoured only where it is exact for this job
   if (e->forced_variant >= 0 && variant_ok(jp, e->forced_variant) &&
       walk_max_blocks(e->forced_variant, 256, jp->step, e->num_sms) > 0)
@@ -468,7 +473,7 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
   // long enough that per-prime setup does not dominate the comparison
   const uint32_t cap_steps = 4096;
-  int best = 0;
+  int best = -1;
   float best_ms = 1e30f;
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
     if (!variant_ok(jp, v)) continue;
@@ -488,6 +493,8 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
     }
   }
   CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
+  if (best < 0)  // a twin job with s < 32 and p above 2^(32+s)
+    return set_err(PPS_ERR_NOT_IMPLEMENTED, "no walk kernel for this job on the prime-list path");
   e->tuned_variant[cls] = best;
   return best;
 }
@@ -671,12 +678,6 @@ static int run_twin_job(pps_engine* e, const pps_job_params* jp, pps_factor* out
   return rc;
 }
 
-static int refuse_twin(const pps_job_params* jp) {
-  if (jp && jp->sign == PPS_SIGN_TWIN)
-    return set_err(PPS_ERR_NOT_IMPLEMENTED, "twin jobs run through pps_run_job / pps_run_batch");
-  return PPS_OK;
-}
-
 extern "C" int pps_run_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap,
                            size_t* nout, pps_job_stats* st) {
   if (!e || !jp) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
@@ -732,7 +733,6 @@ extern "C" int pps_check_primes_device(pps_engine* e, const pps_job_params* jp, 
                                        size_t np, pps_factor* out, size_t cap, size_t* nout,
                                        pps_job_stats* st) {
   if (!e || !jp || (!d_P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
-  if (int rc = refuse_twin(jp)) return rc;
   CU(cudaSetDevice(e->device));
   size_t hit_cap = 1u << 20, fac_cap = 1u << 18;
   for (int attempt = 0; attempt < 4; ++attempt) {
@@ -756,7 +756,6 @@ extern "C" int pps_check_primes(pps_engine* e, const pps_job_params* jp, const u
                                 pps_factor* out, size_t cap, size_t* nout, pps_job_stats* st) {
   if (!e || !jp || (!P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
   int rc;
-  if ((rc = refuse_twin(jp))) return rc;
   CU(cudaSetDevice(e->device));
   if ((rc = e->P.ensure(np ? np : 1))) return rc;
   if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
@@ -774,7 +773,6 @@ extern "C" int pps_check_primes_raw(pps_engine* e, const pps_job_params* jp, con
   if (!e || !jp || (!P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
   if (np > 0xffffffffull) return set_err(PPS_ERR_INVALID_PARAM, "too many primes for one call");
   int rc;
-  if ((rc = refuse_twin(jp))) return rc;
   CU(cudaSetDevice(e->device));
   if ((rc = e->P.ensure(np ? np : 1))) return rc;
   if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));

@@ -58,7 +58,7 @@ struct pps_engine {
   cudaEvent_t ev[8] = {};
   uint64_t batch_span = 1ull << 31;
   int forced_variant = -1;
-  int tuned_variant[2] = {-1, -1};  // [step==32]
+  int tuned_variant[4] = {-1, -1, -1, -1};  // [(step == 32) + 2 * twin]
   uint64_t launches = 0;
 
   // sieving primes (ascending odd primes <= base_limit), u32

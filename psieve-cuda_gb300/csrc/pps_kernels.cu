@@ -407,9 +407,15 @@ __device__ __forceinline__ void q_step(uint32_t& klo, uint32_t& khi, uint32_t pl
   }
 }
 
+// A twin job's candidates carry their side in idx bit 31 (set: k*2^n+1).
+constexpr uint32_t HIT_SIDE_PROTH = 0x80000000u;
+
 // SH: the small-p window (K < 2^sh_t or the low bits in sh_mask zero) in place
 // of the hi-word window, for p far below 2^(64 - bits(kmax)).
-template <int TEST, int U, int MINB, int FORM = 0, bool SH = false>
+// TW: a twin job: the walk holds K = 2^-n, the -1 side's value, and tests
+// p - K, the +1 side's, at the same step (the reference's twin build walks
+// once for both sides too, pps/app.c:1071-1107).
+template <int TEST, int U, int MINB, int FORM = 0, bool SH = false, bool TW = false>
 __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
   __shared__ uint32_t q_ent[WQ_WARPS][WQ_CAP];
   __shared__ uint64_t q_p[WQ_WARPS][32];
@@ -437,17 +443,27 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
       const uint64_t x = inv_pow2(nmin, p, ps);
       const uint64_t K = a.proth ? p - x : x;
       uint32_t klo = lo32(K), khi = hi32(K);
+      // twin: p - K is below the window bound `lim` iff K > p - lim, and its low
+      // bits are zero iff K's equal p's (lim = 0 stands for 2^64)
+      uint64_t tw_above = 0;
+      uint32_t tw_low = 0;
+      if (TW) {
+        const uint64_t lim = SH ? (1ull << sh_t) : (win_hi == 0xffffffffu ? 0ull : ((uint64_t)win_hi + 1ull) << 32);
+        tw_above = (lim != 0ull && p > lim) ? p - lim : 0ull;
+        tw_low = plo & win_mask;
+      }
       for (uint32_t b = 0; b < full; ++b) {
         uint32_t acc = 0xffffffffu;
         bool f = false;
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           if (TEST == 0) acc = min(acc, min(SH ? __funnelshift_rc(klo, khi, sh_t) : khi, klo & win_mask));
-          else if (TEST == 1) f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
+          else if (TEST == 1) f |= (SH ? __funnelshift_rc(klo, khi, sh_t) == 0u : khi <= win_hi) | ((klo & win_mask) == 0u);
           else f |= khi <= bound_hi;
+          if (TW) f |= (mk64(klo, khi) > tw_above) | ((klo & win_mask) == tw_low);
           q_step<FORM>(klo, khi, plo, phi, pinv, sh);
         }
-        if (TEST == 0) f = acc == 0u;
+        if (TEST == 0) f |= acc == 0u;
         if (f) {
           const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
           if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | b;
@@ -484,8 +500,13 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         const uint32_t oplo = lo32(op), ophi = hi32(op), opinv = lo32(ops);
 #pragma unroll 1
         for (uint32_t u = 0; u < nblk; ++u) {
-          record_exact(klo, khi, n0 + s * u, op, a.idx_base + (uint32_t)(base + owner), a.kmin, a.kmax,
-                       a.nmax, a.hits, a.hit_count, a.hit_cap, s);
+          const uint32_t idx = a.idx_base + (uint32_t)(base + owner);
+          record_exact(klo, khi, n0 + s * u, op, idx, a.kmin, a.kmax, a.nmax, a.hits, a.hit_count, a.hit_cap, s);
+          if (TW) {
+            const uint64_t v = op - mk64(klo, khi);
+            record_exact(lo32(v), hi32(v), n0 + s * u, op, idx | HIT_SIDE_PROTH, a.kmin, a.kmax, a.nmax, a.hits,
+                         a.hit_count, a.hit_cap, s);
+          }
           q_step<FORM>(klo, khi, oplo, ophi, opinv, sh);
         }
       }
@@ -499,8 +520,13 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
       const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
 #pragma unroll 1
       for (uint32_t t = 0; t < nsteps; ++t) {
-        record_exact(klo, khi, nmin + s * t, p, a.idx_base + (uint32_t)pi, a.kmin, a.kmax, a.nmax,
-                     a.hits, a.hit_count, a.hit_cap, s);
+        const uint32_t idx = a.idx_base + (uint32_t)pi;
+        record_exact(klo, khi, nmin + s * t, p, idx, a.kmin, a.kmax, a.nmax, a.hits, a.hit_count, a.hit_cap, s);
+        if (TW) {
+          const uint64_t v = p - mk64(klo, khi);
+          record_exact(lo32(v), hi32(v), nmin + s * t, p, idx | HIT_SIDE_PROTH, a.kmin, a.kmax, a.nmax, a.hits,
+                       a.hit_count, a.hit_cap, s);
+        }
         q_step<FORM>(klo, khi, plo, phi, pinv, sh);
       }
     }
@@ -520,7 +546,8 @@ static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
     {"chain-window-u16-block"}, {"queue-min-u8"}, {"queue-window-u8"}, {"queue-bound-u8"},
     {"queue-min-u16"}, {"queue-bound-u16"}, {"queue-min-u8-r40"}, {"queue-bound-u8-r40"},
     {"queue-window-u8-r40"}, {"queue-smallp-u8"}, {"queue-shift-min-u8"}, {"queue-shift-smallp-u8"},
-    {"queue-shift-smallp-u16"},
+    {"queue-shift-smallp-u16"}, {"twin-window-u8"}, {"twin-smallp-u8"}, {"twin-shift-window-u8"},
+    {"twin-shift-smallp-u8"},
 };
 
 const char* walk_variant_name(int v) {
@@ -554,6 +581,10 @@ static walk_fn pick(int v) {
     case 19: return S32 ? nullptr : k_walk32q<0, 8, 8, 1, false>;
     case 20: return S32 ? nullptr : k_walk32q<0, 8, 8, 1, true>;
     case 21: return S32 ? nullptr : k_walk32q<0, 16, 8, 1, true>;
+    case 22: return S32 ? k_walk32q<1, 8, 8, 0, false, true> : nullptr;
+    case 23: return S32 ? k_walk32q<1, 8, 8, 0, true, true> : nullptr;
+    case 24: return S32 ? nullptr : k_walk32q<1, 8, 8, 1, false, true>;
+    case 25: return S32 ? nullptr : k_walk32q<1, 8, 8, 1, true, true>;
   }
   return nullptr;
 }
@@ -593,6 +624,8 @@ __global__ void k_filter(FilterArgs a) {
   if (nh > a.hit_cap) nh = a.hit_cap;
   for (uint32_t h = warp; h < nh; h += nwarps) {
     const pps_hit x = a.hits[h];
+    // a twin job's candidates say their side; every other job has one
+    const int32_t c = a.sign == PPS_SIGN_TWIN ? ((x.idx & HIT_SIDE_PROTH) ? 1 : -1) : a.sign;
     bool ok = (x.k == a.kstep * (x.k / a.kstep) + a.koffset) && x.n >= a.nmin && x.n < a.nmax;
     if (ok && a.in_keys) {
       // the input file's bit of (k, n), every lane the same search
@@ -614,7 +647,7 @@ __global__ void k_filter(FilterArgs a) {
           const uint32_t q = a.small_q[i];
           const uint32_t kr = (uint32_t)(x.k % q);
           const uint32_t t = (kr * pow2_mod_small(x.n, q)) % q;
-          div = ((t + (uint32_t)((int32_t)q + a.sign)) % q) == 0u;
+          div = ((t + (uint32_t)((int32_t)q + c)) % q) == 0u;
         }
         if (__any_sync(0xffffffffu, div)) break;
       }
@@ -627,7 +660,7 @@ __global__ void k_filter(FilterArgs a) {
         f.p = x.p;
         f.k = x.k;
         f.n = x.n;
-        f.c = a.sign;
+        f.c = c;
         a.out[pos] = f;
       }
     }

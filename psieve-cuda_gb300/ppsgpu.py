@@ -31,7 +31,7 @@ PPS_ERR_TIMEOUT = -303
 PPS_ERR_BUSY = -304
 PPS_ERR_NOT_FOUND = -305
 PPS_ERR_CANCELLED = -306
-PPS_NUM_VARIANTS = 22
+PPS_NUM_VARIANTS = 26
 PPS_SIGN_TWIN = 2  # both sides from one walk (the reference's twin build)
 
 FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u8"), ("n", "<u4"), ("c", "<i4")])

@@ -21,6 +21,20 @@ def _gpu_lines(pps, engine, spec):
     return lines_of(pps.factors_to_tuples(fac)), st
 
 
+def _gpu_lines_primes(pps, engine, ora, spec):
+    """Through the prime-list entry point (the one-job walk kernels for every
+    side, twin included)."""
+    jp = pps.normalize(**spec)
+    fac, st = engine.check_primes(jp, ora.sieve_range(jp.pmin, jp.pmax, jp.qmax))
+    return lines_of(pps.factors_to_tuples(fac)), st
+
+
+def ppsgpu_variants() -> int:
+    import ppsgpu
+
+    return ppsgpu.PPS_NUM_VARIANTS
+
+
 @pytest.mark.parametrize("name", FAST_CASES)
 def test_reference_cases(pps, engine, ref_cases, name):
     case = ref_cases[name]
@@ -53,20 +67,24 @@ def test_kat49_planted(pps, engine, kat49):
             assert want in got
 
 
-@pytest.mark.parametrize("variant", list(range(18)))
+@pytest.mark.parametrize("variant", list(range(ppsgpu_variants())))
 def test_every_walk_variant_matches_oracle(pps, engine, ora, variant):
     specs = [
         dict(pmin=10**12, pmax=10**12 + 3 * 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=5000),
+        # s = 32 (forced) with the small-p window: p near 2^50, kmax < 2^7
+        dict(pmin=1 << 50, pmax=(1 << 50) + 2 * 10**6, kmin=3, kmax=99, nmin=1000, nmax=20000),
         dict(pmin=42 * 10**12, pmax=42 * 10**12 + 3 * 10**6, kmin=1201, kmax=9999, nmin=2000000,
              nmax=2040000),
         dict(pmin=(1 << 62) - (1 << 26), pmax=(1 << 62) - (1 << 26) + 2 * 10**6, kmin=3, kmax=9999,
              nmin=100000, nmax=140000, sign=-1),
     ]
+    if variant >= 22:  # the twin kernels walk twin jobs (both sides)
+        specs = [dict(s, sign=pps.PPS_SIGN_TWIN) for s in specs]
     engine.set_variant(variant)
     ran = 0
     try:
         for spec in specs:
-            got, st = _gpu_lines(pps, engine, spec)
+            got, st = _gpu_lines_primes(pps, engine, ora, spec)
             want, cnt, _ = ora.run(ora.normalize(**spec))
             assert got == lines_of(ora.tuples(want)), (variant, spec)
             assert st.primes == cnt

@@ -68,9 +68,13 @@ def test_twin_in_the_serving_loop(pps, engine, twin_cases):
             assert res.primes == twin_cases[n]["count"], n
 
 
-def test_twin_refused_on_host_prime_paths(pps, engine):
-    jp = pps.normalize(pmin=10**12, pmax=10**12 + 10**6, kmin=1201, kmax=9999, nmin=2000, nmax=3000,
-                       sign=pps.PPS_SIGN_TWIN)
-    with pytest.raises(pps.PPSError) as ei:
-        engine.check_primes(jp, np.array([10**12 + 39], dtype=np.uint64))
-    assert ei.value.code == pps.PPS_ERR_NOT_IMPLEMENTED
+def test_twin_on_the_prime_list_path(pps, engine, ora, twin_cases):
+    """pps_check_primes with a twin job: the one-job twin kernels (both sides
+    per step, the side carried by each candidate)."""
+    for name in ("twin_wide_n", "twin_wide_n3", "twin_small"):
+        case = twin_cases[name]
+        jp = twin_params(pps, case["args"])
+        primes = ora.sieve_range(jp.pmin, jp.pmax, jp.qmax)
+        fac, st = engine.check_primes(jp, primes)
+        assert lines_of(pps.factors_to_tuples(fac)) == sorted(set(case["lines"])), name
+        assert st.primes == case["count"] and st.variant >= 22, name
