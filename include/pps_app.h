@@ -23,7 +23,12 @@
 extern "C" {
 #endif
 
+#ifdef PPS_TWIN
+/* the twin build (tpsieve, pps/app.h:35): no -R, both sides at once */
+#define PPS_APP_SHORT_OPTS "k:K:n:N:i:f:b:d:m:M:s:T"
+#else
 #define PPS_APP_SHORT_OPTS "k:K:n:N:i:f:b:d:m:M:s:R"
+#endif
 
 /* pps/app.h:73-84 */
 void app_banner(void);

@@ -92,11 +92,14 @@ def build(verbose: bool = False) -> dict[str, Path]:
     if plugin_src.exists():
         plib = OUT / "libppsgpu_app.so"
         deps = [plugin_src, lib] + sorted(HOST.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
-        if _stale(plib, deps):
-            _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-Wextra", "-fPIC", "-shared",
-                  f"-I{INCLUDE}", f"-I{HOST}", str(plugin_src), "-o", str(plib), f"-L{OUT}",
-                  "-lppsgpu", "-Wl,-rpath,$ORIGIN", "-lpthread"])
-        out["libppsgpu_app"] = plib
+        # the plugin, and its twin build (the reference's tpsieve: -DSEARCH_TWIN)
+        for name, defs in (("libppsgpu_app", []), ("libppsgpu_app_twin", ["-DPPS_TWIN"])):
+            plib = OUT / f"{name}.so"
+            if _stale(plib, deps):
+                _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-Wextra", "-fPIC", "-shared", *defs,
+                      f"-I{INCLUDE}", f"-I{HOST}", str(plugin_src), "-o", str(plib), f"-L{OUT}",
+                      "-lppsgpu", "-Wl,-rpath,$ORIGIN", "-lpthread"])
+            out[name] = plib
     return out
 
 

@@ -29,9 +29,21 @@ void bmsg(const char *msg);
 void bexit(int status);
 char *bmprefix();
 
+/* PPS_TWIN builds the twin plugin (the reference's tpsieve, -DSEARCH_TWIN:
+   pps/app.h:20-45, pps/app.c:53-55): both sides from one walk, k == 3 mod 6
+   by default, no -R. */
+#ifdef PPS_TWIN
+#define PPS_APP_NAME "tpsieve"
+#define FACTORS_FILENAME_DEFAULT "tpfactors.txt"
+#define KSTEP_DEFAULT 6u
+#define KOFFSET_DEFAULT 3u
+#else
 #define PPS_APP_NAME "ppsieve"
-#define PPS_APP_VERSION "gb300-0.1"
 #define FACTORS_FILENAME_DEFAULT "ppfactors.txt"
+#define KSTEP_DEFAULT 2u
+#define KOFFSET_DEFAULT 1u
+#endif
+#define PPS_APP_VERSION "gb300-0.1"
 #define ERR_FOPEN (-108)
 #define ERR_INVALID_PARAM (-178)
 #define ERR_SCANF (-140)
@@ -52,7 +64,7 @@ static unsigned int factor_count = 0;
 static int print_factors = 1;
 static int device_opt = -1;
 static unsigned int user_cthread_count = 0;
-static unsigned int kstep = 2, koffset = 1;
+static unsigned int kstep = KSTEP_DEFAULT, koffset = KOFFSET_DEFAULT;
 static pps_job_params job;
 static pthread_mutex_t factors_mutex = PTHREAD_MUTEX_INITIALIZER;
 
@@ -161,7 +173,9 @@ int app_parse_option(int opt, char *arg, const char *source)
       if (koffset >= kstep) koffset = kstep / 2;
       break;
     case 's': status = parse_u32(&koffset, arg, 1, (1u << 31) - 1); break;
+#ifndef PPS_TWIN
     case 'R': search_proth = -1; break;
+#endif
   }
   return status;
 }
@@ -177,7 +191,9 @@ void app_help(void)
   printf("-m --mthreads=M    Force M threads or blocks/multiprocessor.\n");
   printf("-n --nmin=N0\n");
   printf("-N --nmax=N1       Sieve for primes k*2^n+/-1 with N0 <= n <= N1\n");
+#ifndef PPS_TWIN
   printf("-R --riesel        Sieve for primes k*2^n-1 instead of +1.\n");
+#endif
   printf("-d --device=N      Use GPU N instead of 0-threads\n");
 }
 
@@ -193,9 +209,19 @@ void app_init(void)
   spec.kmax = kmax;
   spec.nmin = nmin;
   spec.nmax = nmax;
+#ifdef PPS_TWIN
+  spec.sign = PPS_SIGN_TWIN;
+#else
   spec.sign = search_proth;
+#endif
   spec.kstep = kstep;
   spec.koffset = koffset;
+#ifdef PPS_TWIN
+  if (input_filename != NULL) {
+    bmsg("The twin build's input formats are not supported\n");
+    bexit(-150);
+  }
+#endif
   if (input_filename != NULL) {
     /* pps/app.c:661-663 and 726-738: the file fills the bounds the command
        line left open, and becomes the output rule */

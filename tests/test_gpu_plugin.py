@@ -96,3 +96,35 @@ def test_plugin_rejects_like_reference(driver, tmp_path):
                         "-K1000000000001", "-n2000", "-N3000"], capture_output=True, text=True)
     assert r.returncode == 3 and "bexit(-178)" in r.stderr
     assert "kmax < pmin" in r.stderr
+
+
+@pytest.fixture(scope="module")
+def twin_driver(pps, tmp_path_factory):
+    out = tmp_path_factory.mktemp("plugin_twin") / "plugin_driver_twin"
+    libdir = Path(pps.LIB_PATH).parent
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-DPPS_TWIN", f"-I{ROOT / 'include'}", str(HARNESS), "-o",
+                    str(out), f"-L{libdir}", "-lppsgpu_app_twin", "-lppsgpu", f"-Wl,-rpath,{libdir}"],
+                   check=True)
+    return out
+
+
+@pytest.mark.parametrize("name", ["twin_wide_n", "twin_wide_n3", "twin_small", "twin_all_odd_k"])
+def test_twin_plugin_factor_file(twin_driver, tmp_path, ora, name):
+    """The twin build of the plugin (tpsieve) against the reference's own twin
+    build run with the same options (tests/golden/twin_cases.json)."""
+    import json
+
+    case = json.loads((GOLDEN / "twin_cases.json").read_text())[name]
+    spec = args_to_spec(case["args"])
+    params = ora.normalize(**dict(spec, sign=2))
+    primes = ora.sieve_range(params.pmin, params.pmax, params.qmax)
+    pf = tmp_path / "primes.bin"
+    primes.astype("<u8").tofile(pf)
+    ff = tmp_path / "factors.txt"
+    args = [a for a in case["args"] if not a.startswith(("-p", "-P"))]
+    r = subprocess.run([str(twin_driver), str(pf), f"-p{params.pmin}", f"-P{params.pmax}", *args,
+                        f"-f{ff}", "-m1"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr
+    lines = sorted(l for l in ff.read_text().splitlines() if "|" in l) if ff.exists() else []
+    assert lines == case["lines"]
+    assert f"count={case['count']}," in r.stdout
