@@ -329,6 +329,9 @@ def run_gpu(args) -> None:
     lib = ppsgpu.load()
     eng = ppsgpu.Engine(local)
     eng.set_batch_span(SPAN)
+    if args.walk_variant >= 0:
+        # a fixed walk kernel (for profiling runs, whose timing would sway the tuner)
+        eng.set_variant(args.walk_variant)
 
     def slice_params(i: int):
         lo = C2["pmin"] + i * SPAN
@@ -528,6 +531,8 @@ def main() -> None:
     ap.add_argument("--profile", type=int, nargs=2, metavar=("SPAN", "NWIDTH"))
     ap.add_argument("--profile-reps", type=int, default=1)
     ap.add_argument("--variant", type=int, default=5)
+    ap.add_argument("--walk-variant", type=int, default=-1,
+                    help="fix the walk kernel of the configuration-2 jobs (default: tuned)")
     ap.add_argument("--sweep", action="store_true")
     ap.add_argument("--profile-batched", action="store_true")
     ap.add_argument("--sweep-span", type=int, default=1 << 28)
