@@ -494,7 +494,12 @@ def run_sweep(args) -> None:
     import ppsgpu
 
     eng = ppsgpu.Engine(0)
-    spec = dict(C2, pmax=C2["pmin"] + args.sweep_span, nmax=C2["nmin"] + args.sweep_nwidth)
+    base = C2
+    if args.sweep_config == 3:  # Riesel at 62-bit primes, n from 100,000
+        base = dict(pmin=(1 << 62) - (1 << 34), kmin=3, kmax=9999, nmin=100000, sign=-1)
+    elif args.sweep_config == 1:
+        base = dict(pmin=10**12, kmin=1201, kmax=9999, nmin=2000)
+    spec = dict(base, pmax=base["pmin"] + args.sweep_span, nmax=base["nmin"] + args.sweep_nwidth)
     jp = ppsgpu.normalize(**spec)
     res = {}
     for v in range(ppsgpu.PPS_NUM_VARIANTS):
@@ -537,6 +542,7 @@ def main() -> None:
     ap.add_argument("--profile-batched", action="store_true")
     ap.add_argument("--sweep-span", type=int, default=1 << 28)
     ap.add_argument("--sweep-nwidth", type=int, default=100000)
+    ap.add_argument("--sweep-config", type=int, default=2, choices=[1, 2, 3])
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
