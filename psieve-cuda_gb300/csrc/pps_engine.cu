@@ -471,8 +471,9 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
     return e->forced_variant;
   if (e->tuned_variant[cls] >= 0 && variant_ok(jp, e->tuned_variant[cls])) return e->tuned_variant[cls];
   const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
-  // long enough that per-prime setup does not dominate the comparison
-  const uint32_t cap_steps = 4096;
+  // long enough that per-prime setup and launch timing do not sway the comparison
+  // (about 2.5 ms per timed launch at 2e12 steps/s)
+  const uint32_t cap_steps = 16384;
   int best = -1;
   float best_ms = 1e30f;
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
