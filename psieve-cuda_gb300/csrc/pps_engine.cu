@@ -460,6 +460,15 @@ int walk_variant_exact(const pps_job_params* jp, int v) { return variant_ok(jp, 
 int set_error_text(int code, const char* msg) { return set_err(code, "%s", msg); }
 }  // namespace pps
 
+// PPS_TUNE_LOG=1 in the environment prints the tuner's timings to stderr.
+static bool tune_log() {
+  static const bool on = [] {
+    const char* v = getenv("PPS_TUNE_LOG");
+    return v && *v && *v != '0';
+  }();
+  return on;
+}
+
 // Time each walk variant on the first `np` resident primes with a capped n
 // range and keep the fastest for this step class.
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
@@ -488,6 +497,7 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
     CU(cudaEventSynchronize(e->ev[7]));
     float ms = 0;
     CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
+    if (tune_log()) fprintf(stderr, "pps tune: step %u variant %d (%s): %.3f ms\n", jp->step, v, walk_variant_name(v), ms);
     if (ms < best_ms) {
       best_ms = ms;
       best = v;
