@@ -473,16 +473,20 @@ static bool tune_log() {
 // range and keep the fastest for this step class.
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
                     uint64_t np) {
-  const int cls = (jp->step == 32 ? 1 : 0) + (jp->sign == PPS_SIGN_TWIN ? 2 : 0);
+  // jobs are told apart by the set of variants exact for them (step size, side,
+  // window kind, bound test): a choice is reused only within the same set
+  uint32_t cls = 0;
+  for (int v = 0; v < PPS_NUM_VARIANTS; ++v) cls |= variant_ok(jp, v) ? (1u << v) : 0u;
   // a forced variant is honoured only where it is exact for this job
   if (e->forced_variant >= 0 && variant_ok(jp, e->forced_variant) &&
       walk_max_blocks(e->forced_variant, 256, jp->step, e->num_sms) > 0)
     return e->forced_variant;
-  if (e->tuned_variant[cls] >= 0 && variant_ok(jp, e->tuned_variant[cls])) return e->tuned_variant[cls];
+  for (const auto& t : e->tuned_variant)
+    if (t.first == cls) return t.second;
   const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
   // long enough that per-prime setup and launch timing do not sway the comparison
-  // (about 2.5 ms per timed launch at 2e12 steps/s)
-  const uint32_t cap_steps = 16384;
+  // (about 1.3 ms per timed launch at 2e12 steps/s)
+  const uint32_t cap_steps = 8192;
   int best = -1;
   float best_ms = 1e30f;
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
@@ -506,7 +510,7 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
   if (best < 0)  // a twin job with s < 32 and p above 2^(32+s)
     return set_err(PPS_ERR_NOT_IMPLEMENTED, "no walk kernel for this job on the prime-list path");
-  e->tuned_variant[cls] = best;
+  e->tuned_variant.emplace_back(cls, best);
   return best;
 }
 

@@ -58,7 +58,8 @@ struct pps_engine {
   cudaEvent_t ev[8] = {};
   uint64_t batch_span = 1ull << 31;
   int forced_variant = -1;
-  int tuned_variant[4] = {-1, -1, -1, -1};  // [(step == 32) + 2 * twin]
+  // tuned walk variant per set of exact variants (bit v: variant v is exact)
+  std::vector<std::pair<uint32_t, int>> tuned_variant;
   uint64_t launches = 0;
 
   // sieving primes (ascending odd primes <= base_limit), u32
