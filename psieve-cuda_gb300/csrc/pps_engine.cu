@@ -481,12 +481,19 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   if (e->forced_variant >= 0 && variant_ok(jp, e->forced_variant) &&
       walk_max_blocks(e->forced_variant, 256, jp->step, e->num_sms) > 0)
     return e->forced_variant;
-  for (const auto& t : e->tuned_variant)
-    if (t.first == cls) return t.second;
   const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
   // long enough that per-prime setup and launch timing do not sway the comparison
   // (about 1.3 ms per timed launch at 2e12 steps/s)
   const uint32_t cap_steps = 8192;
+  // a choice is reused for jobs of the same kind whose sample is not much larger
+  // (a choice timed on a few primes or steps would not hold for a long job)
+  const uint64_t work = sample * std::min<uint64_t>(std::max<uint32_t>(jp->nmax - jp->nmin, 1) / jp->step + 1, cap_steps);
+  size_t slot = e->tuned_variant.size();
+  for (size_t i = 0; i < e->tuned_variant.size(); ++i)
+    if (e->tuned_variant[i].mask == cls) {
+      if (work <= 4 * e->tuned_variant[i].work) return e->tuned_variant[i].variant;
+      slot = i;
+    }
   int best = -1;
   float best_ms = 1e30f;
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
@@ -510,7 +517,8 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
   if (best < 0)  // a twin job with s < 32 and p above 2^(32+s)
     return set_err(PPS_ERR_NOT_IMPLEMENTED, "no walk kernel for this job on the prime-list path");
-  e->tuned_variant.emplace_back(cls, best);
+  if (slot == e->tuned_variant.size()) e->tuned_variant.push_back({});
+  e->tuned_variant[slot] = {cls, best, work};
   return best;
 }
 

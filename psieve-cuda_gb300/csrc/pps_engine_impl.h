@@ -58,8 +58,14 @@ struct pps_engine {
   cudaEvent_t ev[8] = {};
   uint64_t batch_span = 1ull << 31;
   int forced_variant = -1;
-  // tuned walk variant per set of exact variants (bit v: variant v is exact)
-  std::vector<std::pair<uint32_t, int>> tuned_variant;
+  // tuned walk variant per set of exact variants (bit v: variant v is exact),
+  // with the work (primes x steps) of the sample it was timed on
+  struct Tuned {
+    uint32_t mask;
+    int variant;
+    uint64_t work;
+  };
+  std::vector<Tuned> tuned_variant;
   uint64_t launches = 0;
 
   // sieving primes (ascending odd primes <= base_limit), u32
