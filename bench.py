@@ -2,12 +2,12 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-Workload (BASELINE configuration 2, "large-n Proth"): odd k in [1201, 9999],
+Workload ("large-n Proth"): odd k in [1201, 9999],
 n in [2,000,000, 3,000,000), primes p in [4.2e13, 4.2e13 + 1e11).  One step is
 one pass of the hot path over one batch: the device sieve of the next 2^31-wide
 slice of that p range (about 6.8e7 primes), the walk of every prime over the
 whole n range, and the output filter.  Step i takes slice i, so the timed steps
-cover K consecutive slices of the configuration's range (47 slices make the whole
+cover K consecutive slices of the workload's range (47 slices make the whole
 range).  Inputs are generated on the device (the slice's primes are 1.1 GB,
 larger than the 129 MB L2, so no flush is needed between steps).
 
@@ -41,10 +41,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "psieve-cuda_gb300"))
 
 METRIC = "primes/sec & n-steps/sec, k<10^4 n 2M–3M; batched vs plain GPU; serve p50/p99"
-C2 = dict(pmin=42 * 10**12, pmax=42 * 10**12 + 10**11, kmin=1201, kmax=9999, nmin=2000000,
+LARGE_N = dict(pmin=42 * 10**12, pmax=42 * 10**12 + 10**11, kmin=1201, kmax=9999, nmin=2000000,
           nmax=3000000)
 SPAN = 1 << 31
-WORKLOAD = ("config 2 large-n Proth: p in [4.2e13, 4.2e13+1e11), odd k in [1201, 9999], "
+WORKLOAD = ("large-n Proth: p in [4.2e13, 4.2e13+1e11), odd k in [1201, 9999], "
             "n in [2e6, 3e6); one step = one 2^31-wide p slice")
 
 
@@ -133,7 +133,7 @@ class Clocks:
 def _traffic_from_profile() -> float | None:
     """DRAM bytes per prime of the walk kernel from the committed ncu summary
     (the walk reads each prime's 16 B once, whatever the n range)."""
-    f = ROOT / "profiles" / "k_walk32q_c2.md"
+    f = ROOT / "profiles" / "k_walk32q_large_n.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -152,14 +152,14 @@ def _measured_peaks() -> dict:
 
 def cpu_sample(seconds_target: float = 10.0, nthreads: int | None = None) -> dict:
     """Time the CPU restatement of the reference path on a bounded sample of the
-    workload (a p sub-range at the start of the configuration's range)."""
+    workload (a p sub-range at the start of its range)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
     nthreads = nthreads or oracle.threads()
     width = 2 * 10**6
     while True:
-        spec = dict(C2, pmax=C2["pmin"] + width)
+        spec = dict(LARGE_N, pmax=LARGE_N["pmin"] + width)
         p = oracle.normalize(**spec)
         t0 = time.perf_counter()
         _, count, _ = oracle.run(p, nthreads)
@@ -167,7 +167,7 @@ def cpu_sample(seconds_target: float = 10.0, nthreads: int | None = None) -> dic
         if dt >= seconds_target * 0.5 or width >= 10**9:
             break
         width = int(width * min(8.0, max(1.5, seconds_target / max(dt, 1e-3))))
-    steps = (C2["nmax"] - C2["nmin"] + p.nstep - 1) // p.nstep
+    steps = (LARGE_N["nmax"] - LARGE_N["nmin"] + p.nstep - 1) // p.nstep
     return {"value": count / dt, "unit": "primes/s", "cores": nthreads, "kind": "port",
             "sample": f"p in [4.2e13, 4.2e13+{width}) = {count} primes, full n range, "
                       f"{dt:.2f} s on {nthreads} threads",
@@ -175,7 +175,7 @@ def cpu_sample(seconds_target: float = 10.0, nthreads: int | None = None) -> dic
 
 
 def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
-    """Configuration 4: `count` heterogeneous jobs from `seed`, as plain one-job
+    """The mixed-job workload: `count` heterogeneous jobs from `seed`, as plain one-job
     runs (pps_run_job each) and as one batched persistent run (pps_run_batch);
     the per-job results must be identical."""
     import numpy as np
@@ -200,7 +200,7 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
     per, bst = eng.run_batch(jobs)
     t_batch = time.perf_counter() - t0
     identical = len(per) == len(plain) and all(np.array_equal(a, b) for a, b in zip(per, plain))
-    return {"workload": f"{count} mixed jobs, seed {seed} (config 4 distribution); {repaired} "
+    return {"workload": f"{count} mixed jobs, seed {seed} (the mixed-job distribution); {repaired} "
                         "jobs had pmin raised to meet the reference's 2^(64-nstep) <= pmin rule",
             "primes": int(bst.primes), "steps": int(bst.steps), "factors": int(bst.factors),
             "plain_s": t_plain, "batched_s": t_batch,
@@ -211,15 +211,15 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
 
 
 def run_other_configs(eng) -> dict:
-    """Configurations 1 (in full) and 3 (one 2^31-wide slice) through pps_run_job,
+    """The small Proth range in full and one 2^31-wide slice of the 62-bit Riesel range through pps_run_job,
     timed after one warm-up run each (walk tuning per step class)."""
     import ppsgpu
 
     out = {}
     cases = {
-        "config1_full": dict(pmin=10**12, pmax=10**12 + 2 * 10**8, kmin=1201, kmax=9999, nmin=2000,
+        "small_proth_full": dict(pmin=10**12, pmax=10**12 + 2 * 10**8, kmin=1201, kmax=9999, nmin=2000,
                              nmax=3000),
-        "config3_slice": dict(pmin=(1 << 62) - (1 << 34), pmax=(1 << 62) - (1 << 34) + SPAN, kmin=3,
+        "riesel62_slice": dict(pmin=(1 << 62) - (1 << 34), pmax=(1 << 62) - (1 << 34) + SPAN, kmin=3,
                               kmax=9999, nmin=100000, nmax=1000000, sign=-1),
     }
     for name, spec in cases.items():
@@ -235,8 +235,8 @@ def run_other_configs(eng) -> dict:
 
 
 def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -> dict:
-    """Configuration 5: Poisson arrivals at each rate for `window` seconds of
-    jobs from the configuration-4 distribution, submitted to the serving loop
+    """The serving loop: Poisson arrivals at each rate for `window` seconds of
+    jobs from the mixed-job distribution, submitted to the serving loop
     (pps_server_*); every submitted job is waited for.  Reports per rate the
     aggregate primes/s (submission of the first job to the last result) and the
     p50/p99 latency (submission to result ready) of the jobs."""
@@ -281,7 +281,7 @@ def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -
                              "primes_per_s": primes / elapsed, "factors": factors,
                              "p50_ms": rank(0.50), "p99_ms": rank(0.99)})
         st = srv.stats()
-    return {"workload": f"Poisson arrivals, {window:g} s per rate, jobs of the configuration-4 "
+    return {"workload": f"Poisson arrivals, {window:g} s per rate, jobs of the mixed-job "
                         f"distribution (seed {seed})",
             "rates": per_rate, "waves": int(st.waves), "busy_ms": st.busy_ms,
             "completed": int(st.completed), "failed": int(st.failed)}
@@ -334,11 +334,11 @@ def run_gpu(args) -> None:
         eng.set_variant(args.walk_variant)
 
     def slice_params(i: int):
-        lo = C2["pmin"] + i * SPAN
-        hi = min(C2["pmax"], lo + SPAN)
-        return ppsgpu.normalize(**dict(C2, pmin=lo, pmax=hi))
+        lo = LARGE_N["pmin"] + i * SPAN
+        hi = min(LARGE_N["pmax"], lo + SPAN)
+        return ppsgpu.normalize(**dict(LARGE_N, pmin=lo, pmax=hi))
 
-    total_slices = (C2["pmax"] - C2["pmin"] + SPAN - 1) // SPAN
+    total_slices = (LARGE_N["pmax"] - LARGE_N["pmin"] + SPAN - 1) // SPAN
     my_slices = shard_slices(total_slices, ws, rank)
     need = args.warmup + args.steps
     seq = [my_slices[i % len(my_slices)] for i in range(need)]
@@ -464,7 +464,7 @@ def run_profile(args) -> None:
 
     eng = ppsgpu.Engine(0)
     eng.set_variant(args.variant)
-    spec = dict(C2, pmax=C2["pmin"] + args.profile[0], nmax=C2["nmin"] + args.profile[1])
+    spec = dict(LARGE_N, pmax=LARGE_N["pmin"] + args.profile[0], nmax=LARGE_N["nmin"] + args.profile[1])
     for _ in range(args.profile_reps):
         fac, st = eng.run_job(ppsgpu.normalize(**spec))
         print(f"profile job: {st.primes} primes, {st.steps} steps, walk {st.walk_ms:.3f} ms, "
@@ -473,7 +473,7 @@ def run_profile(args) -> None:
 
 
 def run_profile_batched(args) -> None:
-    """The configuration-4 workload through pps_run_batch only (a warm-up batch
+    """The mixed-job workload through pps_run_batch only (a warm-up batch
     of 64 jobs, then the 512 jobs once), for launch lists and captures of the
     batched kernels."""
     import ppsgpu
@@ -494,7 +494,7 @@ def run_sweep(args) -> None:
     import ppsgpu
 
     eng = ppsgpu.Engine(0)
-    base = C2
+    base = LARGE_N
     if args.sweep_config == 3:  # Riesel at 62-bit primes, n from 100,000
         base = dict(pmin=(1 << 62) - (1 << 34), kmin=3, kmax=9999, nmin=100000, sign=-1)
     elif args.sweep_config == 1:
@@ -537,7 +537,7 @@ def main() -> None:
     ap.add_argument("--profile-reps", type=int, default=1)
     ap.add_argument("--variant", type=int, default=5)
     ap.add_argument("--walk-variant", type=int, default=-1,
-                    help="fix the walk kernel of the configuration-2 jobs (default: tuned)")
+                    help="fix the walk kernel of the large-n Proth jobs (default: tuned)")
     ap.add_argument("--sweep", action="store_true")
     ap.add_argument("--profile-batched", action="store_true")
     ap.add_argument("--sweep-span", type=int, default=1 << 28)

@@ -62,17 +62,17 @@ def run_ref(args: list[str], fixed: bool = False, threads: int = 2) -> dict:
 
 def fixed_cases() -> list[tuple[str, list[str], bool]]:
     c = []
-    c.append(("c1_full", ["-p1e12", "-P1000200000000", "-k1201", "-K9999", "-n2000", "-N3000"], False))
+    c.append(("small_proth_full", ["-p1e12", "-P1000200000000", "-k1201", "-K9999", "-n2000", "-N3000"], False))
     c.append(("many_n_test", ["-p42070e9", "-P42070050e6", "-k1201", "-K9999", "-N2000000"], False))
     base = 42 * 10**12
     for i, off in enumerate([0, 25 * 10**9, 50 * 10**9, 75 * 10**9, 10**11 - 2 * 10**6]):
         lo = base + off
-        c.append((f"c2_slice{i}", [f"-p{lo}", f"-P{lo + 2 * 10**6}", "-k1201", "-K9999",
+        c.append((f"large_n_slice{i}", [f"-p{lo}", f"-P{lo + 2 * 10**6}", "-k1201", "-K9999",
                                     "-n2000000", "-N3000000"], False))
     lo3 = (1 << 62) - (1 << 34)
-    c.append(("c3_slice_lo", [f"-p{lo3}", f"-P{lo3 + 10**7}", "-k3", "-K9999", "-n100000",
+    c.append(("riesel62_slice_lo", [f"-p{lo3}", f"-P{lo3 + 10**7}", "-k3", "-K9999", "-n100000",
                               "-N1000000", "-R"], True))
-    c.append(("c3_slice_hi", [f"-p{(1 << 62) - 10**7}", f"-P{1 << 62}", "-k3", "-K9999",
+    c.append(("riesel62_slice_hi", [f"-p{(1 << 62) - 10**7}", f"-P{1 << 62}", "-k3", "-K9999",
                               "-n100000", "-N1000000", "-R"], True))
     # Riesel, small p, many factors
     c.append(("riesel_small", ["-p1e12", "-P1000050000000", "-k1201", "-K9999", "-n2000",
@@ -259,7 +259,7 @@ def main() -> None:
             for k in list(results):
                 if k.startswith("rand") and "rand" in only:
                     del results[k]
-        heavy = {"many_n_test", "c1_full", "c3_slice_lo", "c3_slice_hi"}
+        heavy = {"many_n_test", "small_proth_full", "riesel62_slice_lo", "riesel62_slice_hi"}
 
         def one(case):
             name, args, fixed = case
@@ -281,7 +281,7 @@ def main() -> None:
             lo3 = (1 << 62) - (1 << 34)
             r = run_ref([f"-p{lo3}", f"-P{lo3 + 10**7}", "-k3", "-K9999", "-n100000", "-N1000000",
                          "-R"], fixed=False, threads=8)
-            results["c3_slice_lo_asis"] = r
+            results["riesel62_slice_lo_asis"] = r
         out_json.write_text(json.dumps(results, indent=1, sort_keys=True))
     if "files" in which:
         # The reference's own golden lists, sorted: pps/oldsort.txt (the older,
@@ -303,7 +303,7 @@ def main() -> None:
             ("twin_small", ["-p1e12", "-P1000050000000", "-k1201", "-K9999", "-n2000", "-N3000"]),
             ("twin_all_odd_k", ["-p1e12", "-P1000020000000", "-k3", "-K9999", "-n2000", "-N3000",
                                 "-M2", "-s1"]),
-            ("twin_c2_slice", [f"-p{42 * 10**12}", f"-P{42 * 10**12 + 2 * 10**6}", "-k1201",
+            ("twin_large_n_slice", [f"-p{42 * 10**12}", f"-P{42 * 10**12 + 2 * 10**6}", "-k1201",
                                "-K9999", "-n2000000", "-N3000000"]),
             ("twin_nstep32", [f"-p{2**40}", f"-P{2**40 + 10**7}", "-k3", "-K999", "-n100000",
                               "-N101000", "-M2", "-s1"]),

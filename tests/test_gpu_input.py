@@ -39,6 +39,6 @@ def test_input_files_match_reference(pps, engine):
 
 
 def test_input_rule_is_off_after_reset(pps, engine, ref_cases):
-    case = ref_cases["c1_full"]
+    case = ref_cases["small_proth_full"]
     fac, _ = engine.run_job(pps.normalize(**args_to_spec(case["args"])))
     assert lines_of(pps.factors_to_tuples(fac)) == sorted(set(case["lines"]))

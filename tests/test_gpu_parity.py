@@ -10,8 +10,8 @@ from helpers import args_to_spec, lines_of
 
 pytestmark = pytest.mark.gpu
 
-FAST_CASES = ["c1_full", "many_n_test", "c2_slice0", "c2_slice1", "c2_slice2", "c2_slice3",
-              "c2_slice4", "c3_slice_lo", "c3_slice_hi", "riesel_small", "kstep6_off3", "qmax_1000",
+FAST_CASES = ["small_proth_full", "many_n_test", "large_n_slice0", "large_n_slice1", "large_n_slice2", "large_n_slice3",
+              "large_n_slice4", "riesel62_slice_lo", "riesel62_slice_hi", "riesel_small", "kstep6_off3", "qmax_1000",
               "kround", "nmin_auto", "nstep_clamp_ok", "single_k"]
 
 
@@ -185,7 +185,7 @@ def test_batch_span_does_not_change_results(pps, engine, ora):
     assert np.array_equal(base, small)
 
 
-def test_c2_large_slice_per_line(pps, engine, ora):
+def test_large_n_slice_per_line(pps, engine, ora):
     """Size-independent property at a large size: every reported line is a true
     factor with the output rule satisfied, and the prime fingerprint matches the
     oracle's sieve."""

@@ -26,8 +26,8 @@ def driver(pps, tmp_path_factory):
     return out
 
 
-@pytest.mark.parametrize("name", ["c1_full", "many_n_test", "riesel_small", "kstep6_off3",
-                                  "c2_slice2"])
+@pytest.mark.parametrize("name", ["small_proth_full", "many_n_test", "riesel_small", "kstep6_off3",
+                                  "large_n_slice2"])
 def test_plugin_factor_file(driver, tmp_path, ora, ref_cases, name):
     case = ref_cases[name]
     spec = args_to_spec(case["args"])

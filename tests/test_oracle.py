@@ -13,7 +13,7 @@ from helpers import args_to_spec, lines_of
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
-CHEAP = ["c1_full", "c2_slice0", "c2_slice4", "riesel_small", "kstep6_off3", "qmax_1000",
+CHEAP = ["small_proth_full", "large_n_slice0", "large_n_slice4", "riesel_small", "kstep6_off3", "qmax_1000",
          "kround", "nmin_auto", "nstep_clamp_ok", "single_k"]
 
 
@@ -108,7 +108,7 @@ def test_small_factor_filter_matches_reference_code(ora):
 
 
 def test_oracle_sieve_fingerprints(ora, ref_cases):
-    c1 = ref_cases["c1_full"]
+    c1 = ref_cases["small_proth_full"]
     p = ora.normalize(**args_to_spec(c1["args"]))
     primes = ora.sieve_range(p.pmin, p.pmax, p.qmax)
     assert len(primes) == c1["count"] == 7237499
