@@ -210,7 +210,7 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
             "batched_n_steps_per_s": bst.steps / t_batch}
 
 
-def run_other_configs(eng) -> dict:
+def run_other_workloads(eng) -> dict:
     """The small Proth range in full and one 2^31-wide slice of the 62-bit Riesel range through pps_run_job,
     timed after one warm-up run each (walk tuning per step class)."""
     import ppsgpu
@@ -436,7 +436,7 @@ def run_gpu(args) -> None:
     cpu = None if args.no_cpu else cpu_sample(args.ref_seconds)
     batched = None if args.no_batched else run_mixed(eng, args.mixed_jobs)
     serving = None if args.no_serving else run_serving(window=args.serve_window)
-    others = None if args.no_batched else run_other_configs(eng)
+    others = None if args.no_batched else run_other_workloads(eng)
     line = {"metric": METRIC, "value": value, "unit": "primes/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -450,7 +450,7 @@ def run_gpu(args) -> None:
                          "filter": sum(s.filter_ms for s in stats)},
             "factors": sum(s.factors for s in stats),
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "batched": batched, "serving": serving, "other_configs": others}
+            "batched": batched, "serving": serving, "other_workloads": others}
     print(json.dumps(line), flush=True)
     eng.close()
     if ws > 1:
