@@ -285,6 +285,11 @@ int pps_server_destroy(pps_server *s);
 /* jp: normalised (pps_normalize).  *id identifies the job until its result is taken. */
 int pps_job_submit(pps_server *s, const pps_job_params *jp, uint64_t *id);
 int pps_job_poll(pps_server *s, uint64_t id, int *state);
+/* Cancels a job: a queued job at once, a running one at the end of the wave in
+   flight (its slot and reservation are freed then).  The job ends FAILED with
+   status PPS_ERR_CANCELLED (pps_job_wait returns that code and releases it);
+   a job already finished is left as it is (PPS_OK). */
+int pps_job_cancel(pps_server *s, uint64_t id);
 /* Waits up to timeout_s seconds (< 0: no limit; PPS_ERR_TIMEOUT when it
    expires).  Then *nout = the factor count and res (if given) the job's
    figures.  With out == NULL the job stays (a size query); otherwise the

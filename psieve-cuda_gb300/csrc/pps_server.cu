@@ -49,6 +49,7 @@ struct JobRec {
   std::vector<pps_factor> factors;
   uint64_t primes = 0, sum = 0;  // of the primes below done_p
   uint64_t done_p = 0;           // boundary of the waves completed so far
+  bool cancel = false;           // asked to stop (pps_job_cancel)
   Clock::time_point t_submit, t_done;
 };
 
@@ -109,9 +110,13 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
       s->st.admitted++;
     }
     act = s->active;  // only this thread removes active jobs, so the pointers stay valid
+    for (JobRec* j : act)
+      if (j->cancel && !j->status) j->status = PPS_ERR_CANCELLED;  // no more pieces; retired below
   }
-  pps_engine* e = s->e;
   std::vector<JobRec*> failed;
+  for (JobRec* j : act)
+    if (j->status == PPS_ERR_CANCELLED) failed.push_back(j);
+  pps_engine* e = s->e;
   for (JobRec* j : admitted) {
     j->cursor = j->jp.pmin | 1ull;
     j->done_p = j->jp.pmin;
@@ -311,6 +316,29 @@ extern "C" int pps_job_submit(pps_server* s, const pps_job_params* jp, uint64_t*
     s->jobs[j->id] = std::move(j);
   }
   s->cv_work.notify_one();
+  return PPS_OK;
+}
+
+extern "C" int pps_job_cancel(pps_server* s, uint64_t id) {
+  if (!s) return set_err(PPS_ERR_INVALID_PARAM, "null server");
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) return set_err(PPS_ERR_NOT_FOUND, "no job %llu", (unsigned long long)id);
+    JobRec* j = it->second.get();
+    if (j->state == PPS_JOB_DONE || j->state == PPS_JOB_FAILED) return PPS_OK;
+    if (j->state == PPS_JOB_QUEUED) {
+      s->queue.erase(std::find(s->queue.begin(), s->queue.end(), id));
+      j->state = PPS_JOB_FAILED;
+      j->status = PPS_ERR_CANCELLED;
+      j->t_done = Clock::now();
+      s->st.failed++;
+    } else {
+      j->cancel = true;  // the worker retires it after the wave in flight
+    }
+  }
+  s->cv_work.notify_one();
+  s->cv_done.notify_all();
   return PPS_OK;
 }
 

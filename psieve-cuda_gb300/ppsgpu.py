@@ -229,6 +229,7 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
         "pps_job_submit": (ctypes.c_int, [ctypes.c_void_p, P(JobParams), u64p]),
         "pps_job_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, P(ctypes.c_int)]),
+        "pps_job_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
         "pps_job_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double,
                                         ctypes.c_void_p, ctypes.c_size_t, szp, P(JobResult)]),
         "pps_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, P(ServerStats)]),
@@ -490,6 +491,9 @@ class Server:
         jid = ctypes.c_uint64()
         _check(self.lib, self.lib.pps_job_submit(self.h, ctypes.byref(jp), ctypes.byref(jid)))
         return jid.value
+
+    def cancel(self, jid: int) -> None:
+        _check(self.lib, self.lib.pps_job_cancel(self.h, jid))
 
     def poll(self, jid: int) -> int:
         st = ctypes.c_int()

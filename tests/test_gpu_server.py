@@ -114,3 +114,28 @@ def test_server_checkpoint_resumes_exactly(pps, engine):
     assert (c.sum + tst.prime_sum) % 2**64 == res.prime_sum
     text = pps.checkpoint_format(c)
     assert pps.checkpoint_parse(text, jp).p == c.p
+
+
+def test_server_cancel_queued_and_running(pps, engine):
+    """A cancelled job (queued or running) ends with PPS_ERR_CANCELLED and frees
+    its slot; the server goes on serving, with exact results."""
+    long_job = pps.normalize(pmin=42 * 10**12, pmax=42 * 10**12 + 4 * 10**9, kmin=1201, kmax=9999,
+                             nmin=2000000, nmax=3000000)
+    small = pps.normalize(pmin=10**12, pmax=10**12 + 10**7, kmin=1201, kmax=9999, nmin=2000,
+                          nmax=3000)
+    with pps.Server(0, max_jobs=1, wave_segments=1024) as srv:
+        running = srv.submit(long_job)
+        queued = srv.submit(long_job)  # waits: one slot
+        srv.cancel(queued)
+        assert srv.poll(queued) == pps.PPS_JOB_FAILED
+        srv.cancel(running)
+        for jid in (queued, running):
+            with pytest.raises(pps.PPSError) as ei:
+                srv.wait(jid)
+            assert ei.value.code == pps.PPS_ERR_CANCELLED
+        jid = srv.submit(small)
+        fac, res = srv.wait(jid)
+        st = srv.stats()
+    want, wst = engine.run_job(small)
+    assert pps.factors_to_tuples(fac) == pps.factors_to_tuples(want) and res.primes == wst.primes
+    assert st.failed == 2 and st.running == 0 and st.queued == 0
