@@ -116,6 +116,15 @@ const char *pps_last_error(void);
 /* Library version string. */
 const char *pps_version(void);
 
+/* Test hook (host-side fault injection): after the next `skip` device-buffer
+   allocations of any engine succeed, the `count` after them fail as if device
+   memory were exhausted, so the call that needed them returns
+   PPS_ERR_INSUFFICIENT_RESOURCE; count 0 clears it.  Returns the number of
+   failures injected since the previous call.  No kernel is launched or
+   disturbed.  Replaces nothing in the reference, whose allocation failure path
+   is a retry loop, then exit (pps/appcu.cu:283-324). */
+int pps_debug_fail_allocs(int skip, int count);
+
 /* Apply the reference's option rules (main.c:916-931, main.c:971-972,
    pps/app.c:657-712, pps/appcu.cu:158-204, pps/appcu.cu:236). */
 int pps_normalize(const pps_job_spec *in, pps_job_params *out);

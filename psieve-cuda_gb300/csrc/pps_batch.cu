@@ -690,9 +690,12 @@ int ensure_state(pps_engine* e) {
   BatchState* b = e->batch;
   int rc;
   if (!b->ready) {
+    // (a failure below leaves ready false; the next call resumes here)
     if ((rc = b->tables.ensure(sizeof(WaveTables)))) return rc;
-    if (cudaMallocHost(&b->h_tables, sizeof(WaveTables)) != cudaSuccess)
+    if (!b->h_tables && cudaMallocHost(&b->h_tables, sizeof(WaveTables)) != cudaSuccess) {
+      b->h_tables = nullptr;
       return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "pinned table staging");
+    }
     if ((rc = b->bitmap.ensure((size_t)WAVE_SEGS * SEG_WORDS))) return rc;
     if ((rc = b->seg_count.ensure(WAVE_SEGS)) || (rc = b->seg_off.ensure(WAVE_SEGS)) ||
         (rc = b->chunk_count.ensure(WAVE_SEGS)) || (rc = b->chunk_off.ensure(WAVE_SEGS)) ||
@@ -706,8 +709,10 @@ int ensure_state(pps_engine* e) {
     if ((rc = b->tot.ensure(8))) return rc;
     if ((rc = b->counters.ensure(4))) return rc;
     if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
-    if (cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming) != cudaSuccess)
+    if (!b->copied && cudaEventCreateWithFlags(&b->copied, cudaEventDisableTiming) != cudaSuccess) {
+      b->copied = nullptr;
       return set_err(PPS_ERR_CUDA, "event");
+    }
     // job slots at their maximum size once: the captured graph holds these pointers
     if ((rc = b->jobs.ensure(MAX_JOBS)) || (rc = b->job_primes.ensure(MAX_JOBS)) ||
         (rc = b->job_sum.ensure(MAX_JOBS)) || (rc = b->bak_primes.ensure(MAX_JOBS)) ||
@@ -919,7 +924,12 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
   if ((rc = prepare_sieving_primes(e, want, (uint64_t)want * want + 1, &dq, &bt))) return rc;
   const uint32_t nq_all = e->base_count;
   if (b->qm_q != dq || b->qm_n != nq_all) {
-    // a new sieving-prime table: its Barrett constants (the graph is recaptured too)
+    // a new sieving-prime table: its Barrett constants (the graph, which holds
+    // the old qm pointer, is recaptured too)
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->qm_q = nullptr;
+    b->qm_n = 0;
     if ((rc = b->qm.ensure(std::max<uint32_t>(nq_all, 1)))) return rc;
     if (nq_all) {
       k_brecip<<<std::min<uint32_t>((nq_all + 255) / 256, 4096), 256, 0, st>>>(dq, nq_all, b->qm.p);
@@ -1051,9 +1061,9 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
     if (raw <= b->hits.n) break;
     // more candidates than the buffer: grow it (a new graph), put the slot
     // counters back and walk the wave again
-    if ((rc = b->hits.ensure((size_t)raw * 2))) return rc;
-    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->graph) cudaGraphExecDestroy(b->graph);  // it holds the old hits pointer
     b->graph = nullptr;
+    if ((rc = b->hits.ensure((size_t)raw * 2))) return rc;
     if ((rc = restore())) return rc;
     CU(cudaMemsetAsync(b->counters.p, 0, 2 * sizeof(uint32_t), st));
   }

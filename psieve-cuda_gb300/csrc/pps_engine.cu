@@ -38,6 +38,34 @@ int set_err(int code, const char* fmt, ...) {
 }
 
 extern "C" const char* pps_last_error(void) { return g_err; }
+
+// ---------------------------------------------------- fault injection
+// After `skip` more device-buffer allocations succeed, the next `count` fail
+// (host side only: no kernel is launched or disturbed); used to test that every
+// error path leaves the engine, the batched form and the serving loop usable.
+static std::mutex g_fail_mu;
+static long g_fail_skip = 0, g_fail_pending = 0, g_fail_done = 0;
+
+bool alloc_fault_injected() {
+  std::lock_guard<std::mutex> lk(g_fail_mu);
+  if (g_fail_pending <= 0) return false;
+  if (g_fail_skip > 0) {
+    --g_fail_skip;
+    return false;
+  }
+  --g_fail_pending;
+  ++g_fail_done;
+  return true;
+}
+
+extern "C" int pps_debug_fail_allocs(int skip, int count) {
+  std::lock_guard<std::mutex> lk(g_fail_mu);
+  const long done = g_fail_done;
+  g_fail_skip = skip > 0 ? skip : 0;
+  g_fail_pending = count > 0 ? count : 0;
+  g_fail_done = 0;
+  return (int)done;
+}
 extern "C" const char* pps_version(void) { return "ppsgpu-0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------ normalize
@@ -278,6 +306,9 @@ static int ensure_base(pps_engine* e, uint32_t limit, BaseTable* bt) {
     // capacity: pi(limit) < 1.26 limit / ln(limit)
     const size_t cap = (size_t)(1.3 * limit / log((double)limit)) + 1024;
     int rc;
+    // the table is rebuilt from scratch: a failure below leaves no table
+    e->base_limit = 0;
+    e->base_count = 0;
     if ((rc = e->base_q.ensure(cap))) return rc;
     uint64_t filled = 0;
     const uint64_t span = 1ull << 31;
@@ -543,6 +574,7 @@ static int ensure_input_keys(pps_engine* e, const pps_job_params* jp) {
   if (e->in_built && b.kmin == jp->kmin && b.kmax == jp->kmax && b.kstep == jp->kstep &&
       b.koffset == jp->koffset && b.nmin == jp->nmin && b.nmax == jp->nmax)
     return PPS_OK;
+  e->in_built = false;  // until the new table is on the device
   std::vector<uint64_t> keys;
   uint64_t width = 0;
   int rc = input_keys_for_job(e->input, jp, &keys, &width);

@@ -20,7 +20,13 @@ int set_err(int code, const char* fmt, ...);
                      __FILE__, __LINE__);                                                \
   } while (0)
 
-// Device buffer that only grows (contents are not preserved on growth).
+// Host-side fault injection (pps_debug_fail_allocs): true when this device
+// allocation is to fail as if device memory were exhausted.
+bool alloc_fault_injected();
+
+// Device buffer that only grows (contents are not preserved on growth).  A
+// failed growth leaves it empty (p null, n 0): whatever cached a pointer into
+// it must be invalidated before the call.
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
@@ -31,6 +37,9 @@ struct DevBuf {
     p = nullptr;
     n = 0;
     size_t grow = want + want / 8;
+    if (alloc_fault_injected())
+      return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "cudaMalloc(%zu bytes): injected failure",
+                     grow * sizeof(T));
     cudaError_t e = cudaMalloc(&p, grow * sizeof(T));
     if (e != cudaSuccess) {
       cudaGetLastError();

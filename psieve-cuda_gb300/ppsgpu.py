@@ -198,6 +198,7 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     sig = {
         "pps_last_error": (ctypes.c_char_p, []),
         "pps_version": (ctypes.c_char_p, []),
+        "pps_debug_fail_allocs": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
         "pps_normalize": (ctypes.c_int, [P(JobSpec), P(JobParams)]),
         "pps_engine_create": (ctypes.c_int, [ctypes.c_int, P(ctypes.c_void_p)]),
         "pps_engine_destroy": (None, [ctypes.c_void_p]),
