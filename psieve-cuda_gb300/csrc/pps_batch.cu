@@ -451,26 +451,34 @@ __device__ __forceinline__ void b_record(uint32_t klo, uint32_t khi, uint32_t n,
 }
 
 // Walk-step forms of the batched walk:
-//   0  s == 32: the carry-chain REDC by 2^32;
+//   0  s == 32: the REDC by 2^32 without low-word carries (step_neg32);
 //   1  s < 32 and p <= 2^(32+s): K' = K * 2^(32-s) (< 2^64) through the same
-//      chain, since (K + m p) / 2^s == (K' + m' p) / 2^32 with
+//      step, since (K + m p) / 2^s == (K' + m' p) / 2^32 with
 //      m' = lo32(K') * (-p^-1) mod 2^32 = m * 2^(32-s);
 //   2  s < 32, larger p: the shift-REDC with a wide multiply-add.
-// pinv is lo32(-p^-1) for forms 0 and 1 and that << (32-s) for form 2.
+// pinv is lo32(-p^-1) for forms 0 and 1 and that << (32-s) for form 2; the
+// words (pa, pb) of p are (neg_lo(p), neg_hi(p)) for forms 0 and 1 and
+// (lo32(p), hi32(p)) for form 2 (b_words).
 template <int FORM>
-__device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi, uint32_t pinv,
+__device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t pa, uint32_t pb, uint32_t pinv,
                                        uint32_t s) {
   if (FORM == 0) {
-    step_chain32(klo, khi, plo, phi, pinv);
+    step_neg32(klo, khi, pa, pb, pinv);
   } else if (FORM == 1) {
     const uint32_t sh = 32u - s;
     uint32_t lo = klo << sh, hi = __funnelshift_l(klo, khi, sh);
-    step_chain32(lo, hi, plo, phi, pinv);
+    step_neg32(lo, hi, pa, pb, pinv);
     klo = lo;
     khi = hi;
   } else {
-    step_form0<false>(klo, khi, plo, phi, pinv, s);
+    step_form0<false>(klo, khi, pa, pb, pinv, s);
   }
+}
+
+template <int FORM>
+__device__ __forceinline__ void b_words(uint64_t p, uint32_t* pa, uint32_t* pb) {
+  *pa = FORM == 2 ? lo32(p) : neg_lo(p);
+  *pb = FORM == 2 ? hi32(p) : neg_hi(p);
 }
 
 template <int FORM>
@@ -492,7 +500,8 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
   const uint32_t tag = job | (J.proth == 1u ? SIDE_PROTH : 0u);  // the walked value's side
   qp[lane] = p;
   if (valid) {
-    const uint32_t plo = lo32(p), phi = hi32(p);
+    uint32_t pa, pb;
+    b_words<FORM>(p, &pa, &pb);
     const uint32_t pinv_s = b_pinv<FORM>(ps, s);
     const uint64_t x = inv_pow2(J.nmin, p, ps);
     const uint64_t K = J.proth == 1u ? p - x : x;
@@ -506,7 +515,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
       // lim = 0 stands for 2^64 (every value inside)
       const uint64_t lim = WSH ? (1ull << win_sh) : (win_hi == 0xffffffffu ? 0ull : ((uint64_t)win_hi + 1ull) << 32);
       tw_above = (lim != 0ull && p > lim) ? p - lim : 0ull;
-      tw_low = plo & win_mask;
+      tw_low = lo32(p) & win_mask;
     }
     for (uint32_t b = 0; b < full; ++b) {
       bool f = false;
@@ -519,7 +528,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
         else
           f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
         if (TW) f |= (mk64(klo, khi) > tw_above) | ((klo & win_mask) == tw_low);
-        b_step<FORM>(klo, khi, plo, phi, pinv_s, s);
+        b_step<FORM>(klo, khi, pa, pb, pinv_s, s);
       }
       if (f) {
         const uint32_t pos = atomicAdd(qc, 1u);
@@ -552,7 +561,8 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
         K = J.proth == 1u ? op - x : x;
       }
       uint32_t klo = lo32(K), khi = hi32(K);
-      const uint32_t oplo = lo32(op), ophi = hi32(op);
+      uint32_t opa, opb;
+      b_words<FORM>(op, &opa, &opb);
       const uint32_t opinv = b_pinv<FORM>(ops, s);
 #pragma unroll 1
       for (uint32_t u = 0; u < nblk; ++u) {
@@ -561,11 +571,12 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
           const uint64_t v = op - mk64(klo, khi);
           b_record(lo32(v), hi32(v), n0 + s * u, s, op, job | SIDE_PROTH, J, hits, hit_count, hit_cap);
         }
-        b_step<FORM>(klo, khi, oplo, ophi, opinv, s);
+        b_step<FORM>(klo, khi, opa, opb, opinv, s);
       }
     }
   } else if (valid) {
-    const uint32_t plo = lo32(p), phi = hi32(p);
+    uint32_t pa, pb;
+    b_words<FORM>(p, &pa, &pb);
     const uint32_t pinv_s = b_pinv<FORM>(ps, s);
     const uint64_t x = inv_pow2(J.nmin, p, ps);
     const uint64_t K = J.proth == 1u ? p - x : x;
@@ -577,7 +588,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
         const uint64_t v = p - mk64(klo, khi);
         b_record(lo32(v), hi32(v), J.nmin + s * t, s, p, job | SIDE_PROTH, J, hits, hit_count, hit_cap);
       }
-      b_step<FORM>(klo, khi, plo, phi, pinv_s, s);
+      b_step<FORM>(klo, khi, pa, pb, pinv_s, s);
     }
   }
   __syncwarp();

@@ -114,6 +114,26 @@ __device__ __forceinline__ void step_chain32(uint32_t& klo, uint32_t& khi, uint3
   khi = w2;
 }
 
+// Form 3 (s = 32): no carry out of the low words.  Write p = phi1 2^32 - plon
+// with phi1 = phi + 1 and plon = -plo mod 2^32 (plo is odd, so plon = 2^32 - plo).
+// Since m p == -K (mod 2^32), lo32(m plon) == klo, and
+//   K + m p = (khi + m phi1 - hi32(m plon)) 2^32 + (klo - lo32(m plon)),
+// whose low word is exactly zero: K' = khi + m phi1 - hi32(m plon).  The three
+// multiplies are the same as the chain's (m, one high product, one wide
+// product), but the sum needs no [klo != 0] carry and no carry between the
+// hi(m plo) + khi and lo(m phi) words, which lets the compiler keep the
+// remaining 64-bit add/subtract on the integer ALU instead of the multiply pipe.
+__device__ __forceinline__ uint32_t neg_lo(uint64_t p) { return 0u - lo32(p); }  // plon
+__device__ __forceinline__ uint32_t neg_hi(uint64_t p) { return hi32(p) + 1u; }  // phi1 (p < 2^62)
+__device__ __forceinline__ void step_neg32(uint32_t& klo, uint32_t& khi, uint32_t plon, uint32_t phi1,
+                                           uint32_t pinv) {
+  const uint32_t m = klo * pinv;
+  const uint32_t h = __umulhi(m, plon);
+  const uint64_t r = mk64(m * phi1, __umulhi(m, phi1)) + khi - h;
+  klo = lo32(r);
+  khi = hi32(r);
+}
+
 // Form 2: the low product m' plo + (K mod 2^s) 2^(32-s) as one wide
 // multiply-add whose high word is hi32(m' plo) + [m' != 0], then a second wide
 // multiply-add by phi.

@@ -526,22 +526,30 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
       slot = i;
     }
   int best = -1;
-  float best_ms = 1e30f;
+  float best_ms = 1e30f;  // per prime of the sample
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
     if (!variant_ok(jp, v)) continue;
+    // each variant is timed on whole waves of its own grid (one thread per
+    // prime), so that a variant with fewer resident blocks per SM is not timed
+    // with a partly idle last wave
+    const uint64_t wave = (uint64_t)walk_max_blocks(v, 256, jp->step, e->num_sms) * 256;
+    const uint64_t sv = std::min<uint64_t>(sample, wave ? wave : sample);
     CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
-    int rc = run_walk(e, jp, v, dP, dPinv, nullptr, sample, 0, cap_steps);  // warm-up
+    int rc = run_walk(e, jp, v, dP, dPinv, nullptr, sv, 0, cap_steps);  // warm-up
     if (rc) return rc;
     CU(cudaEventRecord(e->ev[6], e->st));
     for (int r = 0; r < 3; ++r)
-      if ((rc = run_walk(e, jp, v, dP, dPinv, nullptr, sample, 0, cap_steps))) return rc;
+      if ((rc = run_walk(e, jp, v, dP, dPinv, nullptr, sv, 0, cap_steps))) return rc;
     CU(cudaEventRecord(e->ev[7], e->st));
     CU(cudaEventSynchronize(e->ev[7]));
     float ms = 0;
     CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
-    if (tune_log()) fprintf(stderr, "pps tune: step %u variant %d (%s): %.3f ms\n", jp->step, v, walk_variant_name(v), ms);
-    if (ms < best_ms) {
-      best_ms = ms;
+    const float per = ms / (float)std::max<uint64_t>(sv, 1);
+    if (tune_log())
+      fprintf(stderr, "pps tune: step %u variant %d (%s): %.3f ms for %llu primes (%.3f ns per prime)\n", jp->step, v,
+              walk_variant_name(v), ms, (unsigned long long)sv, per * 1e6f);
+    if (per < best_ms) {
+      best_ms = per;
       best = v;
     }
   }

@@ -391,17 +391,18 @@ __device__ __forceinline__ void record_exact(uint32_t klo, uint32_t khi, uint32_
   }
 }
 
-// The queued walk step: FORM 0 is the chain REDC by 2^32 (s = 32); FORM 1 walks
-// s < 32 through the same chain on K * 2^(32-s), exact while p <= 2^(32+s)
+// The queued walk step: FORM 0 is the REDC by 2^32 (s = 32) in the form without
+// low-word carries (step_neg32); FORM 1 walks s < 32 through the same step on
+// K * 2^(32-s), exact while p <= 2^(32+s)
 // ((K + m p) / 2^s == (K 2^(32-s) + m 2^(32-s) p) / 2^32).
 template <int FORM>
-__device__ __forceinline__ void q_step(uint32_t& klo, uint32_t& khi, uint32_t plo, uint32_t phi, uint32_t pinv,
+__device__ __forceinline__ void q_step(uint32_t& klo, uint32_t& khi, uint32_t plon, uint32_t phi1, uint32_t pinv,
                                        uint32_t sh) {
   if (FORM == 0) {
-    step_chain32(klo, khi, plo, phi, pinv);
+    step_neg32(klo, khi, plon, phi1, pinv);
   } else {
     uint32_t lo = klo << sh, hi = __funnelshift_l(klo, khi, sh);
-    step_chain32(lo, hi, plo, phi, pinv);
+    step_neg32(lo, hi, plon, phi1, pinv);
     klo = lo;
     khi = hi;
   }
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
     q_p[wib][lane] = p;
     if (valid) {
       const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
-      const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
+      const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = lo32(ps);
       const uint64_t x = inv_pow2(nmin, p, ps);
       const uint64_t K = a.proth ? p - x : x;
       uint32_t klo = lo32(K), khi = hi32(K);
@@ -450,7 +451,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
       if (TW) {
         const uint64_t lim = SH ? (1ull << sh_t) : (win_hi == 0xffffffffu ? 0ull : ((uint64_t)win_hi + 1ull) << 32);
         tw_above = (lim != 0ull && p > lim) ? p - lim : 0ull;
-        tw_low = plo & win_mask;
+        tw_low = lo32(p) & win_mask;
       }
       for (uint32_t b = 0; b < full; ++b) {
         uint32_t acc = 0xffffffffu;
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
           else if (TEST == 1) f |= (SH ? __funnelshift_rc(klo, khi, sh_t) == 0u : khi <= win_hi) | ((klo & win_mask) == 0u);
           else f |= khi <= bound_hi;
           if (TW) f |= (mk64(klo, khi) > tw_above) | ((klo & win_mask) == tw_low);
-          q_step<FORM>(klo, khi, plo, phi, pinv, sh);
+          q_step<FORM>(klo, khi, plon, phi1, pinv, sh);
         }
         if (TEST == 0) f |= acc == 0u;
         if (f) {
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
           K = a.proth ? op - x : x;
         }
         uint32_t klo = lo32(K), khi = hi32(K);
-        const uint32_t oplo = lo32(op), ophi = hi32(op), opinv = lo32(ops);
+        const uint32_t oplon = neg_lo(op), ophi1 = neg_hi(op), opinv = lo32(ops);
 #pragma unroll 1
         for (uint32_t u = 0; u < nblk; ++u) {
           const uint32_t idx = a.idx_base + (uint32_t)(base + owner);
@@ -507,17 +508,18 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
             record_exact(lo32(v), hi32(v), n0 + s * u, op, idx | HIT_SIDE_PROTH, a.kmin, a.kmax, a.nmax, a.hits,
                          a.hit_count, a.hit_cap, s);
           }
-          q_step<FORM>(klo, khi, oplo, ophi, opinv, sh);
+          q_step<FORM>(klo, khi, oplon, ophi1, opinv, sh);
         }
       }
     } else if (valid) {
       // queue overflow (not expected at the designed false-pass rates): each
       // lane re-walks its own prime with the exact test at every step
+      const uint64_t p = q_p[wib][lane];
       const uint64_t ps = neg_inv64(p);
       const uint64_t x = inv_pow2(nmin, p, ps);
       const uint64_t K = a.proth ? p - x : x;
       uint32_t klo = lo32(K), khi = hi32(K);
-      const uint32_t plo = lo32(p), phi = hi32(p), pinv = lo32(ps);
+      const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = lo32(ps);
 #pragma unroll 1
       for (uint32_t t = 0; t < nsteps; ++t) {
         const uint32_t idx = a.idx_base + (uint32_t)pi;
@@ -527,7 +529,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
           record_exact(lo32(v), hi32(v), nmin + s * t, p, idx | HIT_SIDE_PROTH, a.kmin, a.kmax, a.nmax, a.hits,
                        a.hit_count, a.hit_cap, s);
         }
-        q_step<FORM>(klo, khi, plo, phi, pinv, sh);
+        q_step<FORM>(klo, khi, plon, phi1, pinv, sh);
       }
     }
     __syncwarp();
