@@ -125,13 +125,27 @@ __device__ __forceinline__ void step_chain32(uint32_t& klo, uint32_t& khi, uint3
 // remaining 64-bit add/subtract on the integer ALU instead of the multiply pipe.
 __device__ __forceinline__ uint32_t neg_lo(uint64_t p) { return 0u - lo32(p); }  // plon
 __device__ __forceinline__ uint32_t neg_hi(uint64_t p) { return hi32(p) + 1u; }  // phi1 (p < 2^62)
+// (The sum is written as one 64-bit add and subtract in PTX: the compiler then
+// forms m phi1 as one wide multiply and the add/subtract as a carry pair on
+// the integer ALU, with no register moves on the multiply pipe.)
 __device__ __forceinline__ void step_neg32(uint32_t& klo, uint32_t& khi, uint32_t plon, uint32_t phi1,
                                            uint32_t pinv) {
   const uint32_t m = klo * pinv;
-  const uint32_t h = __umulhi(m, plon);
-  const uint64_t r = mk64(m * phi1, __umulhi(m, phi1)) + khi - h;
-  klo = lo32(r);
-  khi = hi32(r);
+  asm("{\n\t"
+      ".reg .u32 h, l2, g2;\n\t"
+      ".reg .u64 t, k, hh;\n\t"
+      "mul.hi.u32 h, %2, %3;\n\t"   // hi(m plon)
+      "mul.lo.u32 l2, %2, %4;\n\t"  // m phi1, low word
+      "mul.hi.u32 g2, %2, %4;\n\t"  // m phi1, high word
+      "mov.b64 t, {l2, g2};\n\t"
+      "cvt.u64.u32 k, %5;\n\t"
+      "cvt.u64.u32 hh, h;\n\t"
+      "add.u64 t, t, k;\n\t"        // + khi
+      "sub.u64 t, t, hh;\n\t"       // - hi(m plon)
+      "mov.b64 {%0, %1}, t;\n\t"
+      "}"
+      : "=r"(klo), "=r"(khi)
+      : "r"(m), "r"(plon), "r"(phi1), "r"(khi));
 }
 
 // Form 2: the low product m' plo + (K mod 2^s) 2^(32-s) as one wide
