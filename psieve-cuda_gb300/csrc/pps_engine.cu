@@ -479,7 +479,14 @@ static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64
   int maxb = walk_max_blocks(v, threads, jp->step, e->num_sms);
   if (maxb <= 0) return set_err(PPS_ERR_CUDA, "walk variant %d unavailable", v);
   uint64_t need = (np_max + threads - 1) / threads;
-  int blocks = (int)std::min<uint64_t>((uint64_t)maxb, need ? need : 1);
+  // The queued walks (variants 10 and up) get one thread per prime: the block
+  // scheduler then hands new primes to whichever SM has finished its blocks, so
+  // every SM keeps its full complement of warps to the end (with a grid of one
+  // resident wave that loops over the primes, the warps the scheduler favours
+  // finish their share early and the SMs run the rest at reduced occupancy).
+  // The older walks keep one resident wave (their ILP forms stride over it).
+  const uint64_t cap = v >= 10 ? 0x7fffffffull : (uint64_t)maxb;
+  int blocks = (int)std::min<uint64_t>(cap, need ? need : 1);
   CU(launch_walk(v, a, blocks, threads, e->st));
   e->launches++;
   return PPS_OK;
