@@ -47,6 +47,10 @@ struct BJob {
   // all zero; 32: K < (win_hi + 1) * 2^32 or the low bits in win_mask zero
   uint32_t win_sh;
   uint32_t shift_ok;  // step < 32 and pmax <= 2^(32+step): walk form 1
+  uint32_t win_u;     // win_hi == 2^win_u - 1 (32: every hi word passes)
+  // bound_hi < 2^32 - 1: the single-bound test (hi word <= bound_hi), exact for
+  // 32-bit steps when kmax < 2^32 and p > kmax 2^43 (false-pass rate < 2^-12)
+  uint32_t bound_hi;
 };
 
 struct BBatch {
@@ -490,7 +494,13 @@ __device__ __forceinline__ uint32_t b_pinv(uint64_t ps, uint32_t s) {
 // steps (and the partial last block) go to the warp's queue and are re-checked
 // exactly once the round's walks are done.  A twin job (TW) walks K = 2^-n, the
 // -1 side's value, and tests p - K, the +1 side's, at the same step.
-template <int FORM, int U, bool WSH, bool TW>
+// Pre-test (TEST), an exact superset of the hits K = k 2^i (k < 2^kb, i < s),
+// kept as a running minimum over the block:
+//   0  the window: K < 2^(32+win_u), i.e. hi >> win_u == 0, or the low bits in
+//      win_mask zero (a hit below the window, or with i past it);
+//   1  the small-p window: K < 2^win_sh (a funnel shift) or the low bits zero;
+//   2  the single bound: hi <= bound_hi (32-bit steps, p > kmax 2^43).
+template <int FORM, int U, int TEST, bool TW>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
                                         uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
                                         uint32_t* hit_count, uint32_t hit_cap) {
@@ -506,7 +516,9 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
     const uint64_t x = inv_pow2(J.nmin, p, ps);
     const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
-    const uint32_t win_hi = J.win_hi, win_mask = J.win_mask, win_sh = J.win_sh;
+    const uint32_t win_hi = J.win_hi, win_mask = J.win_mask, win_sh = J.win_sh, win_u = J.win_u;
+    const uint32_t bound_hi = J.bound_hi;
+    constexpr bool WSH = TEST == 1;
     // twin: p - K is below the window bound `lim` iff K > p - lim, and its low
     // bits are zero iff K's equal p's
     uint64_t tw_above = 0;
@@ -519,17 +531,19 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
     }
     for (uint32_t b = 0; b < full; ++b) {
       bool f = false;
+      uint32_t acc = 0xffffffffu;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        // exact superset of the hits: a hit K = k*2^i with k < 2^kb is either
-        // below the window or has its low (window - kb + 1) bits zero
-        if (WSH)
-          f |= (__funnelshift_rc(klo, khi, win_sh) == 0u) | ((klo & win_mask) == 0u);
+        if (TEST == 0)
+          acc = min(acc, min(__funnelshift_rc(khi, 0u, win_u), klo & win_mask));
+        else if (TEST == 1)
+          acc = min(acc, min(__funnelshift_rc(klo, khi, win_sh), klo & win_mask));
         else
-          f |= (khi <= win_hi) | ((klo & win_mask) == 0u);
+          acc = min(acc, khi);
         if (TW) f |= (mk64(klo, khi) > tw_above) | ((klo & win_mask) == tw_low);
         b_step<FORM>(klo, khi, pa, pb, pinv_s, s);
       }
+      f |= TEST == 2 ? acc <= bound_hi : acc == 0u;
       if (f) {
         const uint32_t pos = atomicAdd(qc, 1u);
         if (pos < BQ_CAP) qe[pos] = (lane << 27) | b;
@@ -597,7 +611,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
 }
 
 template <int U>
-__global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, const BJob* jobs,
+__global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, const BJob* jobs,
                                                          const uint32_t* seg_count, const uint32_t* seg_off,
                                                          const uint32_t* chunk_off, const uint32_t* chunk_seg,
                                                          const uint64_t* P, const uint64_t* Pinv, uint64_t* tot,
@@ -628,19 +642,20 @@ __global__ void __launch_bounds__(BW_THREADS, 6) k_bwalk(const uint8_t* tables, 
       const bool valid = r + lane < count;
       const uint64_t pi = first + r + (valid ? lane : 0u);
       const uint64_t p = P[pi], ps = Pinv[pi];
-#define PPS_BROUND(FORM_, WSH_, TW_)                                                                    \
-  b_round<FORM_, U, WSH_, TW_>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, \
-                               hit_count, hit_cap)
+#define PPS_BROUND(FORM_, TEST_, TW_)                                                                    \
+  b_round<FORM_, U, TEST_, TW_>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, \
+                                hit_count, hit_cap)
 #define PPS_BROUND_F(FORM_)                                                                             \
   do {                                                                                                  \
     if (wsh) {                                                                                          \
-      if (tw) PPS_BROUND(FORM_, true, true); else PPS_BROUND(FORM_, true, false);                       \
+      if (tw) PPS_BROUND(FORM_, 1, true); else PPS_BROUND(FORM_, 1, false);                             \
     } else {                                                                                            \
-      if (tw) PPS_BROUND(FORM_, false, true); else PPS_BROUND(FORM_, false, false);                     \
+      if (tw) PPS_BROUND(FORM_, 0, true); else PPS_BROUND(FORM_, 0, false);                             \
     }                                                                                                   \
   } while (0)
       const bool wsh = J.win_sh < 32u, tw = J.proth == 2u;
-      if (J.step == 32) PPS_BROUND_F(0);
+      if (J.step == 32 && !tw && J.bound_hi != 0xffffffffu) PPS_BROUND(0, 2, false);
+      else if (J.step == 32) PPS_BROUND_F(0);
       else if (J.shift_ok) PPS_BROUND_F(1);
       else PPS_BROUND_F(2);
 #undef PPS_BROUND_F
@@ -805,6 +820,9 @@ BJob make_job(const pps_job_params& jp) {
   J.qmax = jp.qmax;
   J.sign = jp.sign;
   J.chunk = 32;
+  J.win_u = a.win_hi == 0xffffffffu ? 32u : (uint32_t)__builtin_popcount(a.win_hi);
+  J.bound_hi = 0xffffffffu;
+  if (jp.step == 32 && jp.kmax < (1ull << 32) && jp.pmin / jp.kmax >= (1ull << 43)) J.bound_hi = a.bound_hi;
   small_p_window(jp, &J);
   // form 1 keeps K * 2^(32-step) below 2^64: every K < p <= pmax <= 2^(32+step)
   J.shift_ok = jp.step < 32 && (jp.pmax - 1) >> (32 + jp.step) == 0 ? 1u : 0u;

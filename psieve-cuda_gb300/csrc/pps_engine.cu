@@ -507,14 +507,50 @@ static bool tune_log() {
   return on;
 }
 
+// Estimated probability that variant v's pre-test passes a random walk value
+// (a false pass costs an exact re-check of the block).  Window tests pass when
+// K < 2^(32+u) or its low t bits are zero; the small-p window when K < 2^sh_t
+// or its low sh_t+1-kb bits are zero; the single bound when hi <= kmax/2; the
+// low-bit test roughly when K < kmax 2^32.  Twin variants test two values.
+static double pretest_pass_rate(const pps_job_params* jp, int v) {
+  WalkArgs a;
+  fill_walk_args(jp, &a);
+  const double p = (double)jp->pmin, kmax = (double)jp->kmax;
+  const int kb = lg2u64(jp->kmax) + 1;
+  const bool smallp = v == 18 || v == 20 || v == 21 || v == 23 || v == 25;
+  double r;
+  if (v == 12 || v == 14 || v == 16) {
+    r = kmax * 2147483648.0 / p;
+  } else if (v == 7 || v == 8) {
+    r = kmax * 4294967296.0 / p;
+  } else if (smallp) {
+    r = ldexp(1.0, (int)a.sh_t) / p + ldexp(1.0, -((int)a.sh_t + 1 - kb));
+  } else {
+    const int u = a.win_hi == 0xffffffffu ? 32 : __builtin_popcount(a.win_hi);
+    r = ldexp(1.0, 32 + u) / p + (a.win_mask == 0xffffffffu ? ldexp(1.0, -32) : 1.0 / ((double)a.win_mask + 1.0));
+  }
+  if (v >= 22) r *= 2.0;
+  return std::min(r, 1.0);
+}
+
 // Time each walk variant on the first `np` resident primes with a capped n
 // range and keep the fastest for this step class.
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
                     uint64_t np) {
-  // jobs are told apart by the set of variants exact for them (step size, side,
-  // window kind, bound test): a choice is reused only within the same set
-  uint32_t cls = 0;
-  for (int v = 0; v < PPS_NUM_VARIANTS; ++v) cls |= variant_ok(jp, v) ? (1u << v) : 0u;
+  // Candidates: the variants exact for this job whose pre-test passes at most
+  // 1 step in 512 (a block of 8 then stays below 2% re-checked), or every
+  // exact variant where none does.  Without this a choice timed on one job
+  // could be reused for a job of the same kind at much smaller p, where the
+  // same window passes most steps and the warp queues overflow.
+  uint32_t exact = 0, cls = 0;
+  for (int v = 0; v < PPS_NUM_VARIANTS; ++v)
+    if (variant_ok(jp, v)) {
+      exact |= 1u << v;
+      if (pretest_pass_rate(jp, v) <= 1.0 / 512.0) cls |= 1u << v;
+    }
+  if (!cls) cls = exact;
+  // jobs are told apart by that set (step size, side, window kind, bound test,
+  // pass rates): a choice is reused only within the same set
   // a forced variant is honoured only where it is exact for this job
   if (e->forced_variant >= 0 && variant_ok(jp, e->forced_variant) &&
       walk_max_blocks(e->forced_variant, 256, jp->step, e->num_sms) > 0)
@@ -535,7 +571,7 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   int best = -1;
   float best_ms = 1e30f;  // per prime of the sample
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
-    if (!variant_ok(jp, v)) continue;
+    if (!(cls & (1u << v))) continue;
     // each variant is timed on whole waves of its own grid (one thread per
     // prime), so that a variant with fewer resident blocks per SM is not timed
     // with a partly idle last wave
