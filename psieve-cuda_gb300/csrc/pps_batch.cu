@@ -499,7 +499,8 @@ __device__ __forceinline__ uint32_t b_pinv(uint64_t ps, uint32_t s) {
 //   0  the window: K < 2^(32+win_u), i.e. hi >> win_u == 0, or the low bits in
 //      win_mask zero (a hit below the window, or with i past it);
 //   1  the small-p window: K < 2^win_sh (a funnel shift) or the low bits zero;
-//   2  the single bound: hi <= bound_hi (32-bit steps, p > kmax 2^43).
+//   2  the single bound: hi <= bound_hi (32-bit steps, p > kmax 2^43);
+//   3  the window with win_u == 0 (test 0 without the shift).
 template <int FORM, int U, int TEST, bool TW>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
                                         uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
@@ -536,6 +537,8 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
       for (int u = 0; u < U; ++u) {
         if (TEST == 0)
           acc = min(acc, min(__funnelshift_rc(khi, 0u, win_u), klo & win_mask));
+        else if (TEST == 3)
+          acc = min(acc, min(khi, klo & win_mask));
         else if (TEST == 1)
           acc = min(acc, min(__funnelshift_rc(klo, khi, win_sh), klo & win_mask));
         else
@@ -650,10 +653,11 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
     if (wsh) {                                                                                          \
       if (tw) PPS_BROUND(FORM_, 1, true); else PPS_BROUND(FORM_, 1, false);                             \
     } else {                                                                                            \
-      if (tw) PPS_BROUND(FORM_, 0, true); else PPS_BROUND(FORM_, 0, false);                             \
+      if (tw) PPS_BROUND(FORM_, 0, true); else if (u0) PPS_BROUND(FORM_, 3, false);                     \
+      else PPS_BROUND(FORM_, 0, false);                                                                 \
     }                                                                                                   \
   } while (0)
-      const bool wsh = J.win_sh < 32u, tw = J.proth == 2u;
+      const bool wsh = J.win_sh < 32u, tw = J.proth == 2u, u0 = J.win_u == 0u;
       if (J.step == 32 && !tw && J.bound_hi != 0xffffffffu) PPS_BROUND(0, 2, false);
       else if (J.step == 32) PPS_BROUND_F(0);
       else if (J.shift_ok) PPS_BROUND_F(1);
