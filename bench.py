@@ -445,7 +445,10 @@ def run_gpu(args) -> None:
                        "primes_per_step": primes / args.steps,
                        "l2": "inputs larger than L2 (1.1 GB of primes per step), no flush",
                        "variant": stats[-1].variant if stats else None},
-            "n_steps_per_sec": nsteps_rate, "gpu_launches": launches,
+            "n_steps_per_sec": nsteps_rate,
+            # primes x (nmax - nmin) per second: independent of the step size
+            "n_values_per_sec": value * (LARGE_N["nmax"] - LARGE_N["nmin"]),
+            "gpu_launches": launches,
             "phase_ms": {"sieve": sieve_ms, "walk": walk_ms,
                          "filter": sum(s.filter_ms for s in stats)},
             "factors": sum(s.factors for s in stats),
