@@ -95,6 +95,22 @@ def test_every_walk_variant_matches_oracle(pps, engine, ora, variant):
     assert ran >= 1, variant
 
 
+def test_tuner_keeps_choices_apart_by_pass_rate(pps, ora):
+    """A walk variant tuned on one job is not reused for a job of the same step
+    class at much smaller p, where its window would pass most steps: at
+    p = 1e12 with kmax < 2^14 the plain window passes 1 step in 256, so the
+    choice must be a small-p-window variant (20 or 21), and the result exact."""
+    a = dict(pmin=10**13, pmax=10**13 + 2**24, kmin=1201, kmax=9999, nmin=200000, nmax=260000)
+    b = dict(pmin=10**12, pmax=10**12 + 2**24, kmin=1201, kmax=9999, nmin=200000, nmax=260000)
+    with pps.Engine(0) as eng:
+        eng.run_job(pps.normalize(**a))
+        fac, st = eng.run_job(pps.normalize(**b))
+    assert st.variant in (20, 21), st.variant
+    want, cnt, _ = ora.run(ora.normalize(**b))
+    assert lines_of(pps.factors_to_tuples(fac)) == lines_of(ora.tuples(want))
+    assert st.primes == cnt
+
+
 def test_sieve_matches_oracle(engine, ora):
     rng = np.random.default_rng(5)
     for _ in range(6):
