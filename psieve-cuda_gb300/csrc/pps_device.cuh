@@ -76,7 +76,10 @@ __device__ __forceinline__ uint64_t inv_pow2(uint32_t e, uint64_t p, uint64_t ps
 //   (K + m p)/2^s = (K >> s) + m' * phi + hi32(m' * plo) + [m' != 0]
 // (the low words of (K mod 2^s) 2^(32-s) and m' plo sum to 0 or 2^32).
 //
-// Three formulations of the same arithmetic; the autotuner times them.
+// Four formulations of the same arithmetic.  Forms 0-2 serve the older walk
+// kernels (the autotuner times them); the queued and batched walks use form 3
+// (step_neg32), the one without low-word carries, for s = 32 and, on
+// K * 2^(32-s), for s < 32.
 
 // Form 0: one lo multiply, one hi multiply, one wide multiply-add.
 template <bool S32>
