@@ -828,6 +828,18 @@ BJob make_job(const pps_job_params& jp) {
   J.bound_hi = 0xffffffffu;
   if (jp.step == 32 && jp.kmax < (1ull << 32) && jp.pmin / jp.kmax >= (1ull << 43)) J.bound_hi = a.bound_hi;
   small_p_window(jp, &J);
+  // The small-p window costs a funnel shift per step; the plain window (hi
+  // word below 2^u, no shift when u == 0) is kept where it passes at most
+  // 1 step in 1024 and a round's expected queue (32 lanes x nsteps x rate)
+  // stays within half the warp queue.
+  if (J.win_sh < 32) {
+    const double plain = ldexp(1.0, 32 + (int)J.win_u) / (double)jp.pmin +
+                         (a.win_mask == 0xffffffffu ? ldexp(1.0, -32) : 1.0 / ((double)a.win_mask + 1.0));
+    if (plain <= 1.0 / 1024.0 && 32.0 * (double)J.nsteps * plain <= BQ_CAP / 2) {
+      J.win_sh = 32;
+      J.win_mask = a.win_mask;
+    }
+  }
   // form 1 keeps K * 2^(32-step) below 2^64: every K < p <= pmax <= 2^(32+step)
   J.shift_ok = jp.step < 32 && (jp.pmax - 1) >> (32 + jp.step) == 0 ? 1u : 0u;
   return J;
