@@ -137,7 +137,7 @@ namespace pps {
 
 __device__ __forceinline__ const WaveTables* wt(const uint8_t* t) { return (const WaveTables*)t; }
 
-constexpr uint32_t LARGE_Q_PER_ITEM = 8192;  // large sieving primes per work item
+constexpr uint32_t LARGE_Q_PER_ITEM = 256;  // large sieving primes per work item
 
 // per batch: how many of the ascending sieving primes are <= its limit, and
 // its number of large-prime work items (0 past the last batch)
