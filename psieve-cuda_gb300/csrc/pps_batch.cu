@@ -460,7 +460,7 @@ __device__ __forceinline__ void b_record(uint32_t klo, uint32_t khi, uint32_t n,
 //      step, since (K + m p) / 2^s == (K' + m' p) / 2^32 with
 //      m' = lo32(K') * (-p^-1) mod 2^32 = m * 2^(32-s);
 //   2  s < 32, larger p: the shift-REDC with a wide multiply-add.
-// pinv is lo32(-p^-1) for forms 0 and 1 and that << (32-s) for form 2; the
+// pinv is lo32(-p^-1) for form 0 and that << (32-s) for forms 1 and 2; the
 // words (pa, pb) of p are (neg_lo(p), neg_hi(p)) for forms 0 and 1 and
 // (lo32(p), hi32(p)) for form 2 (b_words).
 template <int FORM>
@@ -469,11 +469,7 @@ __device__ __forceinline__ void b_step(uint32_t& klo, uint32_t& khi, uint32_t pa
   if (FORM == 0) {
     step_neg32(klo, khi, pa, pb, pinv);
   } else if (FORM == 1) {
-    const uint32_t sh = 32u - s;
-    uint32_t lo = klo << sh, hi = __funnelshift_l(klo, khi, sh);
-    step_neg32(lo, hi, pa, pb, pinv);
-    klo = lo;
-    khi = hi;
+    step_neg32s(klo, khi, pa, pb, pinv, 32u - s);
   } else {
     step_form0<false>(klo, khi, pa, pb, pinv, s);
   }
@@ -487,7 +483,7 @@ __device__ __forceinline__ void b_words(uint64_t p, uint32_t* pa, uint32_t* pb) 
 
 template <int FORM>
 __device__ __forceinline__ uint32_t b_pinv(uint64_t ps, uint32_t s) {
-  return FORM == 2 ? (lo32(ps) << (32u - s)) : lo32(ps);
+  return FORM == 0 ? lo32(ps) : (lo32(ps) << (32u - s));
 }
 
 // One round: every lane walks one prime of the same job; flagged blocks of U

@@ -131,9 +131,9 @@ __device__ __forceinline__ uint32_t neg_hi(uint64_t p) { return hi32(p) + 1u; } 
 // (The sum is written as one 64-bit add and subtract in PTX: the compiler then
 // forms m phi1 as one wide multiply and the add/subtract as a carry pair on
 // the integer ALU, with no register moves on the multiply pipe.)
-__device__ __forceinline__ void step_neg32(uint32_t& klo, uint32_t& khi, uint32_t plon, uint32_t phi1,
-                                           uint32_t pinv) {
-  const uint32_t m = klo * pinv;
+// (khi_in + m phi1 - hi32(m plon)) into (lo, hi): the carry-free sum.
+__device__ __forceinline__ void neg_sum(uint32_t m, uint32_t khi_in, uint32_t plon, uint32_t phi1, uint32_t& lo,
+                                        uint32_t& hi) {
   asm("{\n\t"
       ".reg .u32 h, l2, g2;\n\t"
       ".reg .u64 t, k, hh;\n\t"
@@ -143,12 +143,30 @@ __device__ __forceinline__ void step_neg32(uint32_t& klo, uint32_t& khi, uint32_
       "mov.b64 t, {l2, g2};\n\t"
       "cvt.u64.u32 k, %5;\n\t"
       "cvt.u64.u32 hh, h;\n\t"
-      "add.u64 t, t, k;\n\t"        // + khi
+      "add.u64 t, t, k;\n\t"        // + khi_in
       "sub.u64 t, t, hh;\n\t"       // - hi(m plon)
       "mov.b64 {%0, %1}, t;\n\t"
       "}"
-      : "=r"(klo), "=r"(khi)
-      : "r"(m), "r"(plon), "r"(phi1), "r"(khi));
+      : "=r"(lo), "=r"(hi)
+      : "r"(m), "r"(plon), "r"(phi1), "r"(khi_in));
+}
+
+__device__ __forceinline__ void step_neg32(uint32_t& klo, uint32_t& khi, uint32_t plon, uint32_t phi1,
+                                           uint32_t pinv) {
+  const uint32_t m = klo * pinv;
+  neg_sum(m, khi, plon, phi1, klo, khi);
+}
+
+// Form 3 for s < 32 with p <= 2^(32+s): the same reduction applied to
+// K 2^(32-s) (< 2^64).  Its high word is the funnel shift of K, and its low word
+// enters only through m = lo32(K 2^(32-s)) (-p^-1) = klo (pinv << (32-s)) mod
+// 2^32, so the shifted low word is never formed: pass pinv_sh = pinv << sh,
+// sh = 32 - s.  (K 2^(32-s) + m p) / 2^32 = (K + (m / 2^(32-s)) p) / 2^s.
+__device__ __forceinline__ void step_neg32s(uint32_t& klo, uint32_t& khi, uint32_t plon, uint32_t phi1,
+                                            uint32_t pinv_sh, uint32_t sh) {
+  const uint32_t hi = __funnelshift_l(klo, khi, sh);
+  const uint32_t m = klo * pinv_sh;
+  neg_sum(m, hi, plon, phi1, klo, khi);
 }
 
 // Form 2: the low product m' plo + (K mod 2^s) 2^(32-s) as one wide

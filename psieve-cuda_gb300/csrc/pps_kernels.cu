@@ -395,17 +395,19 @@ __device__ __forceinline__ void record_exact(uint32_t klo, uint32_t khi, uint32_
 // low-word carries (step_neg32); FORM 1 walks s < 32 through the same step on
 // K * 2^(32-s), exact while p <= 2^(32+s)
 // ((K + m p) / 2^s == (K 2^(32-s) + m 2^(32-s) p) / 2^32).
+// pinv is lo32(-p^-1) for FORM 0 and that << sh for FORM 1 (q_pinv).
 template <int FORM>
 __device__ __forceinline__ void q_step(uint32_t& klo, uint32_t& khi, uint32_t plon, uint32_t phi1, uint32_t pinv,
                                        uint32_t sh) {
-  if (FORM == 0) {
+  if (FORM == 0)
     step_neg32(klo, khi, plon, phi1, pinv);
-  } else {
-    uint32_t lo = klo << sh, hi = __funnelshift_l(klo, khi, sh);
-    step_neg32(lo, hi, plon, phi1, pinv);
-    klo = lo;
-    khi = hi;
-  }
+  else
+    step_neg32s(klo, khi, plon, phi1, pinv, sh);
+}
+
+template <int FORM>
+__device__ __forceinline__ uint32_t q_pinv(uint64_t ps, uint32_t sh) {
+  return FORM == 0 ? lo32(ps) : lo32(ps) << sh;
 }
 
 // A twin job's candidates carry their side in idx bit 31 (set: k*2^n+1).
@@ -440,7 +442,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
     q_p[wib][lane] = p;
     if (valid) {
       const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
-      const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = lo32(ps);
+      const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = q_pinv<FORM>(ps, sh);
       const uint64_t x = inv_pow2(nmin, p, ps);
       const uint64_t K = a.proth ? p - x : x;
       uint32_t klo = lo32(K), khi = hi32(K);
@@ -498,7 +500,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
           K = a.proth ? op - x : x;
         }
         uint32_t klo = lo32(K), khi = hi32(K);
-        const uint32_t oplon = neg_lo(op), ophi1 = neg_hi(op), opinv = lo32(ops);
+        const uint32_t oplon = neg_lo(op), ophi1 = neg_hi(op), opinv = q_pinv<FORM>(ops, sh);
 #pragma unroll 1
         for (uint32_t u = 0; u < nblk; ++u) {
           const uint32_t idx = a.idx_base + (uint32_t)(base + owner);
@@ -519,7 +521,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
       const uint64_t x = inv_pow2(nmin, p, ps);
       const uint64_t K = a.proth ? p - x : x;
       uint32_t klo = lo32(K), khi = hi32(K);
-      const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = lo32(ps);
+      const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = q_pinv<FORM>(ps, sh);
 #pragma unroll 1
       for (uint32_t t = 0; t < nsteps; ++t) {
         const uint32_t idx = a.idx_base + (uint32_t)pi;
