@@ -51,6 +51,8 @@ struct BJob {
   // bound_hi < 2^32 - 1: the single-bound test (hi word <= bound_hi), exact for
   // 32-bit steps when kmax < 2^32 and p > kmax 2^43 (false-pass rate < 2^-12)
   uint32_t bound_hi;
+  // sw_mask != 0: walk form 1 with test 4 (the window K < 2^s read off the step)
+  uint32_t sw_mask;
 };
 
 struct BBatch {
@@ -496,7 +498,9 @@ __device__ __forceinline__ uint32_t b_pinv(uint64_t ps, uint32_t s) {
 //      win_mask zero (a hit below the window, or with i past it);
 //   1  the small-p window: K < 2^win_sh (a funnel shift) or the low bits zero;
 //   2  the single bound: hi <= bound_hi (32-bit steps, p > kmax 2^43);
-//   3  the window with win_u == 0 (test 0 without the shift).
+//   3  the window with win_u == 0 (test 0 without the shift);
+//   4  walk form 1: K < 2^s, i.e. the step's own high word K >> s is zero,
+//      or the low s+1-kb bits of K zero (sw_mask).
 template <int FORM, int U, int TEST, bool TW>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
                                         uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
@@ -514,7 +518,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
     const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
     const uint32_t win_hi = J.win_hi, win_mask = J.win_mask, win_sh = J.win_sh, win_u = J.win_u;
-    const uint32_t bound_hi = J.bound_hi;
+    const uint32_t bound_hi = J.bound_hi, sw_mask = J.sw_mask;
     constexpr bool WSH = TEST == 1;
     // twin: p - K is below the window bound `lim` iff K > p - lim, and its low
     // bits are zero iff K's equal p's
@@ -535,6 +539,12 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
           acc = min(acc, min(__funnelshift_rc(khi, 0u, win_u), klo & win_mask));
         else if (TEST == 3)
           acc = min(acc, min(khi, klo & win_mask));
+        else if (TEST == 4) {
+          const uint32_t hi = __funnelshift_l(klo, khi, 32u - s);
+          acc = min(acc, min(hi, klo & sw_mask));
+          neg_sum(klo * pinv_s, hi, pa, pb, klo, khi);
+          continue;
+        }
         else if (TEST == 1)
           acc = min(acc, min(__funnelshift_rc(klo, khi, win_sh), klo & win_mask));
         else
@@ -656,6 +666,7 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
       const bool wsh = J.win_sh < 32u, tw = J.proth == 2u, u0 = J.win_u == 0u;
       if (J.step == 32 && !tw && J.bound_hi != 0xffffffffu) PPS_BROUND(0, 2, false);
       else if (J.step == 32) PPS_BROUND_F(0);
+      else if (J.shift_ok && !tw && J.sw_mask) PPS_BROUND(1, 4, false);
       else if (J.shift_ok) PPS_BROUND_F(1);
       else PPS_BROUND_F(2);
 #undef PPS_BROUND_F
@@ -838,6 +849,21 @@ BJob make_job(const pps_job_params& jp) {
   }
   // form 1 keeps K * 2^(32-step) below 2^64: every K < p <= pmax <= 2^(32+step)
   J.shift_ok = jp.step < 32 && (jp.pmax - 1) >> (32 + jp.step) == 0 ? 1u : 0u;
+  // Form-1 jobs take test 4 (no shift of its own: the step computes K >> s
+  // anyway) where its pass rate 2^s / pmin + 2^-(s+1-kb) is at most 1.25 times
+  // the rate of the window chosen above and a round's expected queue fits in
+  // half the warp queue.
+  J.sw_mask = 0;
+  if (J.shift_ok && J.proth != 2u && a.sw_mask) {
+    const int kb = floor_lg2(jp.kmax) + 1;
+    const double pmin = (double)jp.pmin;
+    const double sw = ldexp(1.0, (int)jp.step) / pmin + ldexp(1.0, kb - 1 - (int)jp.step);
+    const double cur = J.win_sh < 32
+                           ? ldexp(1.0, (int)J.win_sh) / pmin + ldexp(1.0, kb - 1 - (int)J.win_sh)
+                           : ldexp(1.0, 32 + (int)J.win_u) / pmin +
+                                 (J.win_mask == 0xffffffffu ? ldexp(1.0, -32) : 1.0 / ((double)J.win_mask + 1.0));
+    if (sw <= 1.25 * cur && 32.0 * (double)J.nsteps * sw <= BQ_CAP / 2) J.sw_mask = a.sw_mask;
+  }
   return J;
 }
 

@@ -433,6 +433,10 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
   a->bound_hi = jp->kmax < (1ull << 32) ? (uint32_t)(jp->kmax >> 1) : 0xffffffffu;
   pps::small_p_window_of(jp, &a->sh_t, &a->sh_mask);
   a->shift_ok = jp->step < 32 && ((jp->pmax - 1) >> (32 + jp->step)) == 0 ? 1u : 0u;
+  {
+    const int r = (int)jp->step + 1 - kb;  // a hit with i > s - kb has its low r bits zero
+    a->sw_mask = r <= 0 ? 0u : (r >= 32 ? 0xffffffffu : (1u << r) - 1u);
+  }
 }
 
 static int variant_ok(const pps_job_params* jp, int v) {
@@ -446,7 +450,7 @@ static int variant_ok(const pps_job_params* jp, int v) {
     fill_walk_args(jp, &a);
     const bool shifted = (v >= 19 && v <= 21) || v >= 24, smallp = v == 18 || v == 20 || v == 21 ||
                                                                     v == 23 || v == 25;
-    if (v == 19 && a.win_hi != 0) return 0;  // running minimum: u == 0 window
+    // (variant 19, the window K < 2^s on the step's shifted words, needs only walk form 1)
     if (shifted && !a.shift_ok) return 0;    // shifted chain: s < 32, p <= 2^(32+s)
     if (smallp && a.sh_t >= 32) return 0;    // small-p window
   }
@@ -525,6 +529,8 @@ static double pretest_pass_rate(const pps_job_params* jp, int v) {
     r = kmax * 4294967296.0 / p;
   } else if (smallp) {
     r = ldexp(1.0, (int)a.sh_t) / p + ldexp(1.0, -((int)a.sh_t + 1 - kb));
+  } else if (v == 19) {
+    r = ldexp(1.0, (int)jp->step) / p + ldexp(1.0, kb - 1 - (int)jp->step);
   } else {
     const int u = a.win_hi == 0xffffffffu ? 32 : __builtin_popcount(a.win_hi);
     r = ldexp(1.0, 32 + u) / p + (a.win_mask == 0xffffffffu ? ldexp(1.0, -32) : 1.0 / ((double)a.win_mask + 1.0));

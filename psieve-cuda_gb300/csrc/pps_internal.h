@@ -55,6 +55,8 @@ struct WalkArgs {
   uint32_t bound_hi;        // single-bound pre-test: hi word <= bound_hi
   uint32_t sh_t, sh_mask;   // small-p window: K < 2^sh_t or (lo & sh_mask) == 0; sh_t 32: none
   uint32_t shift_ok;        // step < 32 and pmax <= 2^(32+step): the shifted chain step
+  uint32_t sw_mask;         // steps s < 32: K < 2^s (hi word of K 2^(32-s) zero) or (lo & sw_mask) == 0,
+                            // sw_mask = 2^(s+1-kb) - 1 (0 where s < kb)
   uint32_t idx_base;        // added to the prime index in hit records
   pps_hit* hits;
   uint32_t* hit_count;      // may exceed hit_cap: overflow is detected by host

@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
   __shared__ uint32_t q_cnt[WQ_WARPS];
   const uint64_t np = a.d_np ? *a.d_np : a.np;
   const uint32_t win_hi = a.win_hi, win_mask = SH ? a.sh_mask : a.win_mask, bound_hi = a.bound_hi;
-  const uint32_t sh_t = a.sh_t;
+  const uint32_t sh_t = a.sh_t, sw_mask = a.sw_mask;
   const uint32_t s = FORM == 0 ? 32u : a.step, sh = 32u - s;
   const uint32_t nsteps = a.nsteps, nmin = a.nmin;
   const uint32_t full = nsteps / (uint32_t)U;  // whole blocks of U steps
@@ -460,13 +460,21 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         bool f = false;
 #pragma unroll
         for (int u = 0; u < U; ++u) {
+          if (TEST == 3) {
+            // walk form 1: the window K < 2^s is the step's own high word
+            // (K >> s) being zero; otherwise the low s+1-kb bits of K are zero
+            const uint32_t hi = __funnelshift_l(klo, khi, sh);
+            acc = min(acc, min(hi, klo & sw_mask));
+            neg_sum(klo * pinv, hi, plon, phi1, klo, khi);
+            continue;
+          }
           if (TEST == 0) acc = min(acc, min(SH ? __funnelshift_rc(klo, khi, sh_t) : khi, klo & win_mask));
           else if (TEST == 1) f |= (SH ? __funnelshift_rc(klo, khi, sh_t) == 0u : khi <= win_hi) | ((klo & win_mask) == 0u);
           else f |= khi <= bound_hi;
           if (TW) f |= (mk64(klo, khi) > tw_above) | ((klo & win_mask) == tw_low);
           q_step<FORM>(klo, khi, plon, phi1, pinv, sh);
         }
-        if (TEST == 0) f |= acc == 0u;
+        if (TEST == 0 || TEST == 3) f |= acc == 0u;
         if (f) {
           const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
           if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | b;
@@ -549,7 +557,7 @@ static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
     {"form2-window-u8-block-ilp2"}, {"chain-lowbit-u8-block"}, {"form0-lowbit-u8-block"},
     {"chain-window-u16-block"}, {"queue-min-u8"}, {"queue-window-u8"}, {"queue-bound-u8"},
     {"queue-min-u16"}, {"queue-bound-u16"}, {"queue-min-u8-r40"}, {"queue-bound-u8-r40"},
-    {"queue-window-u8-r40"}, {"queue-smallp-u8"}, {"queue-shift-min-u8"}, {"queue-shift-smallp-u8"},
+    {"queue-window-u8-r40"}, {"queue-smallp-u8"}, {"queue-shift-hiwin-u8"}, {"queue-shift-smallp-u8"},
     {"queue-shift-smallp-u16"}, {"twin-window-u8"}, {"twin-smallp-u8"}, {"twin-shift-window-u8"},
     {"twin-shift-smallp-u8"},
 };
@@ -582,7 +590,7 @@ static walk_fn pick(int v) {
     case 16: return S32 ? k_walk32q<2, 8, 6> : nullptr;
     case 17: return S32 ? k_walk32q<1, 8, 6> : nullptr;
     case 18: return S32 ? k_walk32q<0, 8, 8, 0, true> : nullptr;
-    case 19: return S32 ? nullptr : k_walk32q<0, 8, 8, 1, false>;
+    case 19: return S32 ? nullptr : k_walk32q<3, 8, 8, 1, false>;
     case 20: return S32 ? nullptr : k_walk32q<0, 8, 8, 1, true>;
     case 21: return S32 ? nullptr : k_walk32q<0, 16, 8, 1, true>;
     case 22: return S32 ? k_walk32q<1, 8, 8, 0, false, true> : nullptr;

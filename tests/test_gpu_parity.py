@@ -98,14 +98,15 @@ def test_every_walk_variant_matches_oracle(pps, engine, ora, variant):
 def test_tuner_keeps_choices_apart_by_pass_rate(pps, ora):
     """A walk variant tuned on one job is not reused for a job of the same step
     class at much smaller p, where its window would pass most steps: at
-    p = 1e12 with kmax < 2^14 the plain window passes 1 step in 256, so the
-    choice must be a small-p-window variant (20 or 21), and the result exact."""
+    p = 1e12 with kmax < 2^14 the plain window K < 2^32 passes 1 step in 256, so
+    the choice must be one whose window scales with p (19: K < 2^s; 20, 21: the
+    small-p window), and the result exact."""
     a = dict(pmin=10**13, pmax=10**13 + 2**24, kmin=1201, kmax=9999, nmin=200000, nmax=260000)
     b = dict(pmin=10**12, pmax=10**12 + 2**24, kmin=1201, kmax=9999, nmin=200000, nmax=260000)
     with pps.Engine(0) as eng:
         eng.run_job(pps.normalize(**a))
         fac, st = eng.run_job(pps.normalize(**b))
-    assert st.variant in (20, 21), st.variant
+    assert st.variant in (19, 20, 21), st.variant
     want, cnt, _ = ora.run(ora.normalize(**b))
     assert lines_of(pps.factors_to_tuples(fac)) == lines_of(ora.tuples(want))
     assert st.primes == cnt
