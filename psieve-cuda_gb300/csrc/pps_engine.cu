@@ -544,15 +544,21 @@ static double pretest_pass_rate(const pps_job_params* jp, int v) {
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
                     uint64_t np) {
   // Candidates: the variants exact for this job whose pre-test passes at most
-  // 1 step in 512 (a block of 8 then stays below 2% re-checked), or every
-  // exact variant where none does.  Without this a choice timed on one job
-  // could be reused for a job of the same kind at much smaller p, where the
-  // same window passes most steps and the warp queues overflow.
+  // 1 step in 512 (a block of 8 then stays below 2% re-checked) and, for the
+  // queued walks (variants 10 and up), whose expected flagged blocks per warp
+  // over the whole n range (32 lanes x nsteps x rate) stay within half the warp
+  // queue; or every exact variant where none does.  The tuner times a capped
+  // n range, so without the queue bound it could pick a variant whose queue
+  // overflows on the full range (each lane then re-walks its prime exactly);
+  // and without the rate bound a choice timed on one job could be reused for a
+  // job of the same kind at much smaller p, where its window passes most steps.
+  const double nsteps_full = jp->nmax > jp->nmin ? (double)((jp->nmax - jp->nmin + jp->step - 1) / jp->step) : 0.0;
   uint32_t exact = 0, cls = 0;
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v)
     if (variant_ok(jp, v)) {
       exact |= 1u << v;
-      if (pretest_pass_rate(jp, v) <= 1.0 / 512.0) cls |= 1u << v;
+      const double r = pretest_pass_rate(jp, v);
+      if (r <= 1.0 / 512.0 && (v < 10 || 32.0 * nsteps_full * r <= WALK_QUEUE_CAP / 2)) cls |= 1u << v;
     }
   if (!cls) cls = exact;
   // jobs are told apart by that set (step size, side, window kind, bound test,

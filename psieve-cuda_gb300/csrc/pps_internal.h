@@ -64,6 +64,10 @@ struct WalkArgs {
 };
 
 // Variant v in [0, PPS_NUM_VARIANTS): step formulation x pre-test x unroll.
+// Flagged blocks a warp of the queued walks (variants 10 and up) holds for its
+// exact re-check; beyond it each lane re-walks its prime with the exact test.
+constexpr int WALK_QUEUE_CAP = 512;
+
 const char* walk_variant_name(int v);
 // Pre-test constants of a normalised job, and whether variant v is exact for it
 // (defined in pps_engine.cu).

@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
 // warp's primes finish their walk, the warp re-checks the queued blocks together
 // (one block per lane), recomputing each block's starting value as
 // -/+2^-(nmin + 32 U b) mod p.  The hot loop thus holds no exact-check code.
-constexpr int WQ_CAP = 256;   // queue entries per warp
+constexpr int WQ_CAP = WALK_QUEUE_CAP;   // queue entries per warp
 constexpr int WQ_WARPS = 8;   // warps per 256-thread block
 
 __device__ __forceinline__ void record_exact(uint32_t klo, uint32_t khi, uint32_t n, uint64_t p, uint32_t idx,
