@@ -34,7 +34,7 @@ constexpr uint32_t BATCH_SEGS = 1u << 12;       // segments per batch
 constexpr uint32_t WAVE_BATCHES = WAVE_SEGS;    // at most one batch per segment
 constexpr uint32_t MAX_JOBS = 1u << 16;
 constexpr int BW_THREADS = 256;
-constexpr uint32_t BQ_CAP = 256;  // queued blocks per warp
+constexpr uint32_t BQ_CAP = 512;  // queued blocks per warp
 constexpr uint32_t MAX_CHUNK = 8192;  // primes per work chunk, at most (a multiple of 32)
 
 struct BJob {
