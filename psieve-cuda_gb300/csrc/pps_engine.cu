@@ -448,9 +448,8 @@ static int variant_ok(const pps_job_params* jp, int v) {
   if (v >= 18) {
     WalkArgs a;
     fill_walk_args(jp, &a);
-    const bool shifted = (v >= 19 && v <= 21) || v >= 24, smallp = v == 18 || v == 20 || v == 21 ||
-                                                                    v == 23 || v == 25;
-    // (variant 19, the window K < 2^s on the step's shifted words, needs only walk form 1)
+    const bool shifted = (v >= 19 && v <= 21) || v >= 24, smallp = v == 18 || v == 20 || v == 23 || v == 25;
+    // (variants 19 and 21, the window K < 2^s on the step's shifted words, need only walk form 1)
     if (shifted && !a.shift_ok) return 0;    // shifted chain: s < 32, p <= 2^(32+s)
     if (smallp && a.sh_t >= 32) return 0;    // small-p window
   }
@@ -521,7 +520,7 @@ static double pretest_pass_rate(const pps_job_params* jp, int v) {
   fill_walk_args(jp, &a);
   const double p = (double)jp->pmin, kmax = (double)jp->kmax;
   const int kb = lg2u64(jp->kmax) + 1;
-  const bool smallp = v == 18 || v == 20 || v == 21 || v == 23 || v == 25;
+  const bool smallp = v == 18 || v == 20 || v == 23 || v == 25;
   double r;
   if (v == 12 || v == 14 || v == 16) {
     r = kmax * 2147483648.0 / p;
@@ -529,7 +528,7 @@ static double pretest_pass_rate(const pps_job_params* jp, int v) {
     r = kmax * 4294967296.0 / p;
   } else if (smallp) {
     r = ldexp(1.0, (int)a.sh_t) / p + ldexp(1.0, -((int)a.sh_t + 1 - kb));
-  } else if (v == 19) {
+  } else if (v == 19 || v == 21) {
     r = ldexp(1.0, (int)jp->step) / p + ldexp(1.0, kb - 1 - (int)jp->step);
   } else {
     const int u = a.win_hi == 0xffffffffu ? 32 : __builtin_popcount(a.win_hi);

@@ -558,7 +558,7 @@ static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
     {"chain-window-u16-block"}, {"queue-min-u8"}, {"queue-window-u8"}, {"queue-bound-u8"},
     {"queue-min-u16"}, {"queue-bound-u16"}, {"queue-min-u8-r40"}, {"queue-bound-u8-r40"},
     {"queue-window-u8-r40"}, {"queue-smallp-u8"}, {"queue-shift-hiwin-u8"}, {"queue-shift-smallp-u8"},
-    {"queue-shift-smallp-u16"}, {"twin-window-u8"}, {"twin-smallp-u8"}, {"twin-shift-window-u8"},
+    {"queue-shift-hiwin-u8-r40"}, {"twin-window-u8"}, {"twin-smallp-u8"}, {"twin-shift-window-u8"},
     {"twin-shift-smallp-u8"},
 };
 
@@ -592,7 +592,7 @@ static walk_fn pick(int v) {
     case 18: return S32 ? k_walk32q<0, 8, 8, 0, true> : nullptr;
     case 19: return S32 ? nullptr : k_walk32q<3, 8, 8, 1, false>;
     case 20: return S32 ? nullptr : k_walk32q<0, 8, 8, 1, true>;
-    case 21: return S32 ? nullptr : k_walk32q<0, 16, 8, 1, true>;
+    case 21: return S32 ? nullptr : k_walk32q<3, 8, 6, 1, false>;
     case 22: return S32 ? k_walk32q<1, 8, 8, 0, false, true> : nullptr;
     case 23: return S32 ? k_walk32q<1, 8, 8, 0, true, true> : nullptr;
     case 24: return S32 ? nullptr : k_walk32q<1, 8, 8, 1, false, true>;

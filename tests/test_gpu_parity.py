@@ -99,7 +99,7 @@ def test_tuner_keeps_choices_apart_by_pass_rate(pps, ora):
     """A walk variant tuned on one job is not reused for a job of the same step
     class at much smaller p, where its window would pass most steps: at
     p = 1e12 with kmax < 2^14 the plain window K < 2^32 passes 1 step in 256, so
-    the choice must be one whose window scales with p (19: K < 2^s; 20, 21: the
+    the choice must be one whose window scales with p (19, 21: K < 2^s; 20: the
     small-p window), and the result exact."""
     a = dict(pmin=10**13, pmax=10**13 + 2**24, kmin=1201, kmax=9999, nmin=200000, nmax=260000)
     b = dict(pmin=10**12, pmax=10**12 + 2**24, kmin=1201, kmax=9999, nmin=200000, nmax=260000)
