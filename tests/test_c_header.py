@@ -87,7 +87,7 @@ def test_header_from_c(built, pps, tmp_path):
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=120).stdout
     lines = dict(line.split(" ", 1) for line in out.strip().splitlines())
     assert lines["version"].startswith("ppsgpu")
-    # the reference's rules: nmin from pmin and kmax (pps/app.c:683-694), kmax rounded odd
+    # nmax as given; kmin and kmax already odd, so kept by the rounding of pps/app.c:705-708
     norm = lines["normalize"].split()
     assert norm[0] == "0"
     assert int(norm[4]) == 2000000 and int(norm[6]) == 1201 and int(norm[8]) == 9999
