@@ -91,3 +91,18 @@ def test_pretests_pass_every_candidate():
         # single bound: K = k 2^i with i < 32 has hi word <= kmax / 2
         i = rng.randrange(32)
         assert ((k << i) >> 32) <= kmax >> 1
+
+
+def test_twin_pretest_reads_the_other_side():
+    """Twin walks hold K for one side and test p - K for the other: p - K is
+    below a bound lim iff K > p - lim, and its low bits (mask) are zero iff K's
+    low bits equal p's."""
+    rng = random.Random(5)
+    for _ in range(20000):
+        p = _random_prime_like(rng, rng.randint(33, 62))
+        K = rng.randrange(1, p)
+        lim = 1 << rng.randint(20, 40)
+        mask = (1 << rng.randint(1, 31)) - 1
+        v = p - K
+        assert (v < lim) == (p > lim and K > p - lim or p <= lim)
+        assert ((v & mask) == 0) == ((K & mask) == (p & mask))
