@@ -492,37 +492,6 @@ def run_profile_batched(args) -> None:
     eng.close()
 
 
-def run_sweep(args) -> None:
-    """Walk rate of every kernel variant on the first slice (stderr report)."""
-    import ppsgpu
-
-    eng = ppsgpu.Engine(0)
-    base = LARGE_N
-    if args.sweep_config == 3:  # Riesel at 62-bit primes, n from 100,000
-        base = dict(pmin=(1 << 62) - (1 << 34), kmin=3, kmax=9999, nmin=100000, sign=-1)
-    elif args.sweep_config == 1:
-        base = dict(pmin=10**12, kmin=1201, kmax=9999, nmin=2000)
-    spec = dict(base, pmax=base["pmin"] + args.sweep_span, nmax=base["nmin"] + args.sweep_nwidth)
-    jp = ppsgpu.normalize(**spec)
-    res = {}
-    for v in range(ppsgpu.PPS_NUM_VARIANTS):
-        eng.set_variant(v)
-        eng.run_job(jp)
-        best = None
-        for _ in range(3):
-            _, st = eng.run_job(jp)
-            rate = st.steps / (st.walk_ms * 1e-3)
-            best = max(best or 0, rate)
-        if st.variant != v:
-            print(f"variant {v}: not exact for this job (ran {st.variant})", flush=True)
-            continue
-        res[v] = best
-        print(f"variant {v}: {best:.4e} walk steps/s ({3 * best / 1e12:.3f} Tmul/s)", flush=True)
-    print(f"imad peak: {eng.imad_peak() / 1e12:.3f} Tmul/s", flush=True)
-    print(json.dumps({"sweep": res}), flush=True)
-    eng.close()
-
-
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -541,18 +510,12 @@ def main() -> None:
     ap.add_argument("--variant", type=int, default=5)
     ap.add_argument("--walk-variant", type=int, default=-1,
                     help="fix the walk kernel of the large-n Proth jobs (default: tuned)")
-    ap.add_argument("--sweep", action="store_true")
     ap.add_argument("--profile-batched", action="store_true")
-    ap.add_argument("--sweep-span", type=int, default=1 << 28)
-    ap.add_argument("--sweep-nwidth", type=int, default=100000)
-    ap.add_argument("--sweep-config", type=int, default=2, choices=[1, 2, 3])
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
     elif args.profile_batched:
         run_profile_batched(args)
-    elif args.sweep:
-        run_sweep(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -1,17 +1,21 @@
 /* pps_app.h -- the application plugin hooks served by the GPU plugin
-   (psieve-cuda_gb300/host/app_gpu.c, object _build/app_gpu.o).
+   (psieve-cuda_gb300/host/app_gpu.c, built as _build/libppsgpu_app.so; its twin
+   build, the reference's tpsieve, as _build/libppsgpu_app_twin.so).
 
    Same names, arguments, return values and error behaviour as the reference's
    plugin interface pps/app.h:73-96 (Ken-g6/PSieve-CUDA), so the reference's
    main.c and sieve.c link against this plugin in place of pps/app.c +
    pps/appcu.cu + pps/factor_proth.c.  The plugin reads main.c's globals
-   (main.h:57-60) and reports fatal errors through main.c's bexit().
+   (main.h:57-60), parses option values with main.c's parse_uint64 / parse_uint
+   (putil.h:36-39) and reports fatal errors through main.c's bexit(); an
+   executable that links it provides those symbols, as main.c + putil.c do.
 
    Behaviour differences (by design; outputs are the same lines):
      - the device returns exact (p, k, n) and applies the output rule of
        pps/app.c:159-186 itself, so there is no CPU re-walk of flagged primes;
      - app_thread_fun1() does not pad a partial batch with composites;
-     - -i (input sieve file) is rejected with ERR_NOT_IMPLEMENTED.
+     - -i (input sieve file, NewPGen or ABCD) is read on the host and becomes
+       the output rule on the device (pps/app.c:180-183), as in the reference.
 */
 #ifndef PPS_APP_H
 #define PPS_APP_H

@@ -18,7 +18,12 @@
 //
 // Set-up: the first call on each device (with that device current) looks up
 // the scratch's device address with cudaGetSymbolAddress and copies the small-
-// prime table into it.  Make that first call before any stream capture.
+// prime table into it, on the caller's stream, and waits for that copy before
+// it records the device as set up.  Make that first call before any stream
+// capture.  The address is looked up once per device for the life of the
+// process, so cudaDeviceReset() on a device that has been set up is not
+// supported: a call that finds the table gone (its tag word no longer set)
+// reports PPS_ERR_CUDA instead of returning factors.
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -31,8 +36,12 @@
 
 namespace {
 
+constexpr uint32_t kTableTag = 0x50505351u;  // written with the small-prime table
+
 struct NoallocScratch {
   uint32_t counters[4];  // [0] raw candidates, [1] factors
+  uint32_t table_tag;    // kTableTag once the small-prime table is in place
+  uint32_t pad[3];
   uint16_t small_q[3584];
   pps_hit hits[PPS_NOALLOC_MAX_CANDIDATES];
 };
@@ -67,7 +76,7 @@ void make_small_primes() {
   g_nsmall = n;
 }
 
-int setup(int dev, NoallocScratch** out) {
+int setup(int dev, cudaStream_t st, NoallocScratch** out) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (dev < 0 || dev >= kMaxDevices) return fail(PPS_ERR_NO_DEVICE, "device %d out of range", dev);
   if (g_addr[dev]) {
@@ -79,7 +88,12 @@ int setup(int dev, NoallocScratch** out) {
   cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) return fail(PPS_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
   NoallocScratch* s = (NoallocScratch*)p;
-  e = cudaMemcpy(s->small_q, g_small_host, g_nsmall * sizeof(uint16_t), cudaMemcpyHostToDevice);
+  // on the caller's stream, and complete before any call relies on it (a copy
+  // from pageable memory may return before the device has the data)
+  static const uint32_t tag = kTableTag;
+  e = cudaMemcpyAsync(s->small_q, g_small_host, g_nsmall * sizeof(uint16_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&s->table_tag, &tag, sizeof tag, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(PPS_ERR_CUDA, "small-prime table: %s", cudaGetErrorString(e));
   g_addr[dev] = s;
   *out = s;
@@ -104,10 +118,10 @@ extern "C" int pps_check_primes_noalloc(const pps_job_params* jp, const uint64_t
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(PPS_ERR_NO_DEVICE, "cudaGetDevice: %s", cudaGetErrorString(e));
-  NoallocScratch* s = nullptr;
-  int rc = setup(dev, &s);
-  if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  NoallocScratch* s = nullptr;
+  int rc = setup(dev, st, &s);
+  if (rc) return rc;
   e = cudaMemsetAsync(s->counters, 0, sizeof s->counters, st);
   if (e != cudaSuccess) return fail(PPS_ERR_CUDA, "clear counters: %s", cudaGetErrorString(e));
 
@@ -122,7 +136,9 @@ extern "C" int pps_check_primes_noalloc(const pps_job_params* jp, const uint64_t
     a.hits = s->hits;
     a.hit_count = &s->counters[0];
     a.hit_cap = PPS_NOALLOC_MAX_CANDIDATES;
-    static const int order[] = {13, 10, 2, 1, 0};
+    // queued walks first (32-bit steps: 13, 10; shorter steps: 21, 19), then the
+    // plain block walks, which are exact for every job
+    static const int order[] = {13, 10, 21, 19, 2, 1, 0};
     int v = -1;
     for (int c : order)
       if (walk_variant_exact(jp, c)) {
@@ -133,8 +149,11 @@ extern "C" int pps_check_primes_noalloc(const pps_job_params* jp, const uint64_t
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int maxb = walk_max_blocks(v, 256, jp->step, sms > 0 ? sms : 1);
     if (v < 0 || maxb <= 0) return fail(PPS_ERR_CUDA, "no walk kernel for this job");
+    // the queued walks get one thread per prime (the block scheduler keeps every
+    // SM full to the end); the block walks one resident wave that strides
     const uint64_t need = (np + 255) / 256;
-    const int blocks = (int)(need < (uint64_t)maxb ? need : (uint64_t)maxb);
+    const uint64_t cap = v >= 10 ? 0x7fffffffull : (uint64_t)maxb;
+    const int blocks = (int)(need < cap ? need : cap);
     e = launch_walk(v, a, blocks, 256, st);
     if (e != cudaSuccess) return fail(PPS_ERR_CUDA, "walk launch: %s", cudaGetErrorString(e));
 
@@ -155,10 +174,12 @@ extern "C" int pps_check_primes_noalloc(const pps_job_params* jp, const uint64_t
     e = launch_filter(f, PPS_NOALLOC_MAX_CANDIDATES, st);
     if (e != cudaSuccess) return fail(PPS_ERR_CUDA, "filter launch: %s", cudaGetErrorString(e));
   }
-  uint32_t counts[4] = {0, 0, 0, 0};
+  uint32_t counts[5] = {0, 0, 0, 0, 0};  // the counters and the table tag
   e = cudaMemcpyAsync(counts, s->counters, sizeof counts, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(PPS_ERR_CUDA, "read counters: %s", cudaGetErrorString(e));
+  if (counts[4] != kTableTag)
+    return fail(PPS_ERR_CUDA, "the scratch's small-prime table is gone (cudaDeviceReset is not supported)");
   if (counts[0] > PPS_NOALLOC_MAX_CANDIDATES)
     return fail(PPS_ERR_OVERFLOW, "%u candidates exceed the scratch limit of %u; split the list",
                 counts[0], (unsigned)PPS_NOALLOC_MAX_CANDIDATES);

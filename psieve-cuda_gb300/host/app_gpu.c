@@ -10,7 +10,6 @@
    pps/app.c:551-617, 649-790, 1294-1398 and 124-148.
 */
 #define _GNU_SOURCE
-#include <errno.h>
 #include <inttypes.h>
 #include <pthread.h>
 #include <stdio.h>
@@ -81,72 +80,12 @@ typedef struct {
 
 static app_thread_t threads[MAX_APP_THREADS];
 
-/* ------------------------------------------------------------ number parsing
-   putil.c:86-168: decimal/0x/0 prefixes; K M G T P = 10^3..10^15; k m g t p =
-   2^10..2^50; eN = *10^N; bN = *2^N.  0 ok, -1 unparsable, -2 out of range. */
-static int parse_u64(uint64_t *result, const char *str, uint64_t lo, uint64_t hi)
-{
-  char *tail;
-  unsigned expt = 0;
-  errno = 0;
-  uint64_t num = strtoull(str, &tail, 0);
-  if (errno != 0 || num > hi) return -2;
-  switch (*tail) {
-    case 'P': expt += 3; /* fall through */
-    case 'T': expt += 3; /* fall through */
-    case 'G': expt += 3; /* fall through */
-    case 'M': expt += 3; /* fall through */
-    case 'K': expt += 3;
-      if (tail[1] != '\0') return -1;
-      for (; expt > 0; expt -= 3) {
-        if (num > hi / 1000) return -2;
-        num *= 1000;
-      }
-      break;
-    case 'e': case 'E':
-      expt = (unsigned)strtoul(tail + 1, &tail, 0);
-      if (errno != 0) return -2;
-      if (*tail != '\0') return -1;
-      while (expt-- > 0) {
-        if (num > hi / 10) return -2;
-        num *= 10;
-      }
-      break;
-    case 'p': expt += 10; /* fall through */
-    case 't': expt += 10; /* fall through */
-    case 'g': expt += 10; /* fall through */
-    case 'm': expt += 10; /* fall through */
-    case 'k': expt += 10;
-      if (tail[1] != '\0') return -1;
-      if (num > (hi >> expt)) return -2;
-      num <<= expt;
-      break;
-    case 'b': case 'B':
-      expt = (unsigned)strtoul(tail + 1, &tail, 0);
-      if (errno != 0) return -2;
-      if (*tail != '\0') return -1;
-      while (expt-- > 0) {
-        if (num > (hi >> 1)) return -2;
-        num <<= 1;
-      }
-      break;
-    case '\0':
-      break;
-    default:
-      return -1;
-  }
-  if (num < lo) return -2;
-  *result = num;
-  return 0;
-}
-
-static int parse_u32(unsigned *result, const char *str, unsigned lo, unsigned hi)
-{
-  uint64_t v;
-  int st = parse_u64(&v, str, lo, hi);
-  if (st == 0) *result = (unsigned)v;
-  return st;
-}
+/* Number parsing is main.c's own: putil.c:86-168 parse_uint64 / parse_uint
+   (putil.h:36-39), resolved from the executable like bexit() above, so option
+   values are read exactly as the reference reads them (K M G T P suffixes,
+   k m g t p, eN, bN; 0 ok, -1 unparsable, -2 out of range). */
+int parse_uint(unsigned int *result, const char *str, unsigned int lo, unsigned int hi);
+int parse_uint64(uint64_t *result, const char *str, uint64_t lo, uint64_t hi);
 
 /* ------------------------------------------------------------------- hooks */
 
@@ -160,19 +99,19 @@ int app_parse_option(int opt, char *arg, const char *source)
 {
   int status = 0;
   switch (opt) {
-    case 'k': status = parse_u64(&kmin, arg, 1, ((uint64_t)1 << 62) - 1); break;
-    case 'K': status = parse_u64(&kmax, arg, 1, ((uint64_t)1 << 62) - 1); break;
-    case 'm': status = parse_u32(&user_cthread_count, arg, 1, 1u << 31); break;
-    case 'n': status = parse_u32(&nmin, arg, 1, (1u << 31) - 1); break;
-    case 'N': status = parse_u32(&nmax, arg, 1, (1u << 31) - 1); break;
+    case 'k': status = parse_uint64(&kmin, arg, 1, ((uint64_t)1 << 62) - 1); break;
+    case 'K': status = parse_uint64(&kmax, arg, 1, ((uint64_t)1 << 62) - 1); break;
+    case 'm': status = parse_uint(&user_cthread_count, arg, 1, 1u << 31); break;
+    case 'n': status = parse_uint(&nmin, arg, 1, (1u << 31) - 1); break;
+    case 'N': status = parse_uint(&nmax, arg, 1, (1u << 31) - 1); break;
     case 'i': input_filename = (source == NULL) ? arg : strdup(arg); break;
     case 'f': factors_filename = (source == NULL) ? arg : strdup(arg); break;
-    case 'd': status = parse_u32((unsigned *)&device_opt, arg, 0, INT32_MAX); break;
+    case 'd': status = parse_uint((unsigned *)&device_opt, arg, 0, INT32_MAX); break;
     case 'M':
-      status = parse_u32(&kstep, arg, 1, (1u << 31) - 1);
+      status = parse_uint(&kstep, arg, 1, (1u << 31) - 1);
       if (koffset >= kstep) koffset = kstep / 2;
       break;
-    case 's': status = parse_u32(&koffset, arg, 1, (1u << 31) - 1); break;
+    case 's': status = parse_uint(&koffset, arg, 1, (1u << 31) - 1); break;
 #ifndef PPS_TWIN
     case 'R': search_proth = -1; break;
 #endif

@@ -33,6 +33,8 @@ PPS_ERR_NOT_FOUND = -305
 PPS_ERR_CANCELLED = -306
 PPS_NUM_VARIANTS = 26
 PPS_SIGN_TWIN = 2  # both sides from one walk (the reference's twin build)
+PPS_NOALLOC_MAX_PRIMES = 1 << 24  # per call of pps_check_primes_noalloc
+PPS_NOALLOC_MAX_CANDIDATES = 1 << 16
 
 FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u8"), ("n", "<u4"), ("c", "<i4")])
 HIT_DTYPE = np.dtype([("p", "<u8"), ("k", "<u8"), ("n", "<u4"), ("idx", "<u4")])

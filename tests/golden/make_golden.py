@@ -1,10 +1,12 @@
 """Generate the golden fixtures in tests/golden/ by running the REFERENCE itself.
 
-    make -C oracle ref                      # builds oracle/_ref/ from the reference sources
+    make -C oracle refsrc CHECKOUT=<reference checkout>   # stages its C sources
+    make -C oracle ref                      # builds oracle/_ref/ from them
     python tests/golden/make_golden.py      # (re)writes tests/golden/ref_cases.json, kat49.json
 
-Needs the reference checkout (REF, default /root/reference) only through the
-binaries that `make -C oracle ref` compiled into oracle/_ref/:
+Needs the reference only through the binaries that `make -C oracle ref`
+compiled into oracle/_ref/ (the "files" step also reads the reference's shipped
+golden lists, from the checkout named by PPS_REFERENCE):
   ppsieve_ref        the reference's main.c/sieve.c/pps/app.c/pps/factor_proth.c with
                      the CPU stand-in for pps/appcu.h (every subsection flagged);
   ppsieve_ref_fixed  the same with the 64-bit fix at pps/app.c:1087 (used where
@@ -287,7 +289,10 @@ def main() -> None:
         # The reference's own golden lists, sorted: pps/oldsort.txt (the older,
         # unfiltered many_n_test.sh output) and pps/pps_test_ok.txt; and the
         # many_n_test.sh range as the current reference prints it (from its run).
-        ref_root = Path(os.environ.get("PPS_REFERENCE", "/root/reference"))
+        if not os.environ.get("PPS_REFERENCE"):
+            sys.exit("the files step reads pps/oldsort.txt and pps/pps_test_ok.txt: "
+                     "set PPS_REFERENCE=<reference checkout>")
+        ref_root = Path(os.environ["PPS_REFERENCE"])
         for src, dst in (("pps/oldsort.txt", "oldsort_144.txt"),
                          ("pps/pps_test_ok.txt", "pps_test_ok_15.txt")):
             lines = sorted(l.strip() for l in (ref_root / src).read_text().splitlines()

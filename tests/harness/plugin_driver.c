@@ -9,6 +9,7 @@
 
    usage: plugin_driver PRIMES_FILE -pPMIN -PPMAX [plugin options...]
 */
+#include <errno.h>
 #include <getopt.h>
 #include <inttypes.h>
 #include <stdio.h>
@@ -20,6 +21,56 @@
 int num_threads = 1;
 uint64_t pmin, pmax, pstart;
 unsigned int quiet_opt = 1;
+
+/* main.c's number parser (putil.c parse_uint64 / parse_uint) is the
+   executable's to provide; this stand-in reads the forms the tests pass:
+   decimal or 0x numbers with an optional decimal exponent eN, or one suffix
+   K M G T P (powers of 1000) or k m g t p (powers of 1024).  0 ok,
+   -1 unparsable, -2 out of range. */
+static int scale_checked(uint64_t *v, uint64_t f, unsigned long times, uint64_t hi)
+{
+  while (times--) {
+    if (*v > hi / f) return -2;
+    *v *= f;
+  }
+  return 0;
+}
+
+int parse_uint64(uint64_t *result, const char *str, uint64_t lo, uint64_t hi)
+{
+  static const char dec[] = "KMGTP", bin[] = "kmgtp";
+  char *end;
+  errno = 0;
+  uint64_t v = strtoull(str, &end, 0);
+  if (end == str) return -1;
+  if (errno) return -2;
+  int rc = 0;
+  const char *d;
+  if (*end == 'e' || *end == 'E') {
+    char *e2;
+    unsigned long x = strtoul(end + 1, &e2, 10);
+    if (e2 == end + 1 || *e2) return -1;
+    rc = scale_checked(&v, 10, x, hi);
+  } else if (*end && end[1] == '\0' && (d = strchr(dec, *end)) != NULL) {
+    rc = scale_checked(&v, 1000, (unsigned long)(d - dec) + 1, hi);
+  } else if (*end && end[1] == '\0' && (d = strchr(bin, *end)) != NULL) {
+    rc = scale_checked(&v, 1024, (unsigned long)(d - bin) + 1, hi);
+  } else if (*end) {
+    return -1;
+  }
+  if (rc) return rc;
+  if (v < lo || v > hi) return -2;
+  *result = v;
+  return 0;
+}
+
+int parse_uint(unsigned int *result, const char *str, unsigned int lo, unsigned int hi)
+{
+  uint64_t v;
+  int rc = parse_uint64(&v, str, lo, hi);
+  if (rc == 0) *result = (unsigned int)v;
+  return rc;
+}
 
 void bmsg(const char *msg) { fputs(msg, stderr); }
 char *bmprefix(void) { return ""; }
