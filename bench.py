@@ -21,6 +21,14 @@ roofline: the walk kernel is bound by the 32-bit integer multiply pipe; its
          algorithmic work is 3 multiplies per walk step (one 32 n-values advance
          of one prime); the peak is the multiply-pipe throughput measured in this
          run by pps_measure_imad_peak on the same multiply mix.
+verify : the checker leg, after every timed leg and not timed: the large-n
+         Proth workload (47 slices) and the 62-bit Riesel workload
+         (p in [2^62 - 2^34, 2^62), 8 slices) run in full on the GPU; every
+         factor the bench reported (the full runs, the timed slices, the
+         host-buffer path, the 512-job mix, the served jobs) is verified line by
+         line by the oracle on the host cores, and the prime count and sum of
+         every full-range slice (and of 16 seeded mixed jobs) are compared with
+         the oracle's sieve.
 --impl reference: the reference's CPU algorithm (the committed C restatement in
          oracle/, the reference's own build is not available on the GPU host) on
          all host cores, one bounded sample of the same workload per step.
@@ -200,7 +208,9 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
     per, bst = eng.run_batch(jobs)
     t_batch = time.perf_counter() - t0
     identical = len(per) == len(plain) and all(np.array_equal(a, b) for a, b in zip(per, plain))
-    return {"workload": f"{count} mixed jobs, seed {seed} (the mixed-job distribution); {repaired} "
+    job_primes, job_sums = eng.batch_job_primes(len(jobs))
+    checked = {"jobs": jobs, "lists": per, "job_primes": job_primes, "job_sums": job_sums}
+    return checked, {"workload": f"{count} mixed jobs, seed {seed} (the mixed-job distribution); {repaired} "
                         "jobs had pmin raised to meet the reference's 2^(64-nstep) <= pmin rule",
             "primes": int(bst.primes), "steps": int(bst.steps), "factors": int(bst.factors),
             "plain_s": t_plain, "batched_s": t_batch,
@@ -248,12 +258,13 @@ def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -
     pool, _ = ppsgpu.mixed_jobs(seed=seed, count=need)
     rng = np.random.default_rng(seed)
     per_rate = []
+    served = []  # (job, factors) of every job waited for, for the checker
     with ppsgpu.Server(0) as srv:
         for jp in pool[:8]:  # warm-up: walk tuning, graph capture, sieving primes
             srv.wait(srv.submit(jp))
         nxt = 8
         for rate in rates:
-            ids = []
+            ids, jps = [], []
             t0 = time.perf_counter()
             t = 0.0
             while True:
@@ -263,11 +274,13 @@ def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -
                 delay = t0 + t - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                ids.append(srv.submit(pool[nxt % len(pool)]))
+                jps.append(pool[nxt % len(pool)])
+                ids.append(srv.submit(jps[-1]))
                 nxt += 1
             lat, primes, factors = [], 0, 0
-            for jid in ids:
+            for jid, jp in zip(ids, jps):
                 fac, res = srv.wait(jid)
+                served.append((jp, fac))
                 lat.append(res.latency_ms)
                 primes += res.primes
                 factors += len(fac)
@@ -281,10 +294,116 @@ def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -
                              "primes_per_s": primes / elapsed, "factors": factors,
                              "p50_ms": rank(0.50), "p99_ms": rank(0.99)})
         st = srv.stats()
-    return {"workload": f"Poisson arrivals, {window:g} s per rate, jobs of the mixed-job "
+    return served, {"workload": f"Poisson arrivals, {window:g} s per rate, jobs of the mixed-job "
                         f"distribution (seed {seed})",
             "rates": per_rate, "waves": int(st.waves), "busy_ms": st.busy_ms,
             "completed": int(st.completed), "failed": int(st.failed)}
+
+
+RIESEL62 = dict(pmin=(1 << 62) - (1 << 34), pmax=1 << 62, kmin=3, kmax=9999, nmin=100000, nmax=1000000,
+                sign=-1)
+
+
+class Checker:
+    """The oracle as the checker of what the GPU reported (run after the timed
+    regions, never timed, never the thing measured): per-line verification of
+    factor lists (p prime, p | k*2^n+c, k and n in range, the output rule) and
+    the prime count/sum of whole p ranges against the oracle's sieve, on the
+    host cores in a background thread, so that it overlaps the GPU's full-range
+    runs."""
+
+    def __init__(self, nthreads: int | None = None):
+        from concurrent.futures import ThreadPoolExecutor
+
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+
+        self.ora = oracle
+        self.nthreads = nthreads or max(1, oracle.threads() - 1)
+        self.ex = ThreadPoolExecutor(1)
+        self.verify_futs: dict[str, list] = {}
+        self.fp_futs: dict[str, list] = {}
+
+    def params(self, jp):
+        """The oracle's own normalisation of a job (idempotent on normalised jobs)."""
+        return self.ora.normalize(pmin=jp.pmin, pmax=jp.pmax, kmin=jp.kmin, kmax=jp.kmax, nmin=jp.nmin,
+                                  nmax=jp.nmax, sign=jp.sign, kstep=jp.kstep, koffset=jp.koffset,
+                                  qmax=jp.qmax)
+
+    def verify(self, label: str, jobs_and_lists) -> None:
+        """Queue the per-line verification of (job, factors) pairs under `label`."""
+        import numpy as np
+
+        jobs, rows, job_of = [], [], []
+        for jp, fac in jobs_and_lists:
+            jobs.append(self.params(jp))
+            rows.append(fac)
+            job_of.append(np.full(len(fac), len(jobs) - 1, dtype=np.uint32))
+        if not jobs:
+            return
+        allrows = np.concatenate(rows) if rows else np.zeros(0)
+
+        def work():
+            fails, bad = self.ora.verify_factors(jobs, allrows, np.concatenate(job_of), self.nthreads)
+            return {"lines": int(len(allrows)), "failures": fails,
+                    "first_failures": [[int(allrows[i]["p"]), int(allrows[i]["k"]), int(allrows[i]["n"]),
+                                        int(allrows[i]["c"]), int(bad[i])] for i in np.nonzero(bad)[0][:5]]}
+
+        self.verify_futs.setdefault(label, []).append(self.ex.submit(work))
+
+    def fingerprint(self, label: str, lo: int, hi: int, qmax: int, got_count: int, got_sum: int) -> None:
+        """Queue the oracle's count/sum of [lo, hi) against the GPU's."""
+
+        def work():
+            cnt, sm = self.ora.fingerprint(lo, hi, qmax, self.nthreads)
+            return {"equal": cnt == got_count and sm == (got_sum & (2**64 - 1)), "count": cnt}
+
+        self.fp_futs.setdefault(label, []).append(self.ex.submit(work))
+
+    def results(self) -> dict:
+        out = {}
+        for label in sorted(set(self.verify_futs) | set(self.fp_futs)):
+            r = {}
+            vs = [f.result() for f in self.verify_futs.get(label, [])]
+            if vs:
+                r["verified_factors"] = sum(v["lines"] for v in vs)
+                r["verify_failures"] = sum(v["failures"] for v in vs)
+                first = [x for v in vs for x in v["first_failures"]][:5]
+                if first:
+                    r["first_failures"] = first
+            fs = [f.result() for f in self.fp_futs.get(label, [])]
+            if fs:
+                r["fingerprints_checked"] = len(fs)
+                r["fingerprints_equal"] = all(f["equal"] for f in fs)
+                r["oracle_primes"] = sum(f["count"] for f in fs)
+            out[label] = r
+        self.ex.shutdown()
+        return out
+
+
+def run_full_range(eng, chk: Checker, spec: dict, label: str) -> tuple[dict, dict]:
+    """One workload over its whole p range, one 2^31-wide slice per pps_run_job
+    call: every slice's factors go to the checker's per-line verification and
+    every slice's prime count/sum to its fingerprint.  Returns the factor list of
+    each slice (by index) and a summary."""
+    import ppsgpu
+
+    lists, primes, factors, gpu_s = {}, 0, 0, 0.0
+    nslices = (spec["pmax"] - spec["pmin"] + SPAN - 1) // SPAN
+    for i in range(nslices):
+        lo = spec["pmin"] + i * SPAN
+        hi = min(spec["pmax"], lo + SPAN)
+        jp = ppsgpu.normalize(**dict(spec, pmin=lo, pmax=hi))
+        t0 = time.perf_counter()
+        fac, st = eng.run_job(jp)
+        gpu_s += time.perf_counter() - t0
+        lists[i] = fac
+        primes += st.primes
+        factors += len(fac)
+        chk.verify(label, [(jp, fac)])
+        chk.fingerprint(label, jp.pmin, jp.pmax, jp.qmax, st.primes, st.prime_sum)
+    return lists, {"p_range": [spec["pmin"], spec["pmax"]], "slices": nslices, "primes": primes,
+                   "factors": factors, "gpu_s": gpu_s}
 
 
 def run_reference(args) -> None:
@@ -310,6 +429,51 @@ def run_reference(args) -> None:
                     "d2h_bytes_per_step": 0},
             "n_steps_per_sec": statistics.median(r["n_steps_per_sec"] for r in per_step)}
     print(json.dumps(line), flush=True)
+
+
+def run_checks(eng, args, slice_params, seq, timed_lists, e2e_lists, mixed, served) -> dict:
+    """The checker leg (after every timed leg; not timed): the large-n Proth
+    workload and the 62-bit Riesel workload run in full on the GPU, every
+    factor the bench reported (full runs, timed slices, the host-buffer path,
+    the 512-job mix, the served jobs) is verified line by line by the oracle,
+    and the prime count/sum of every full-range slice and of a seeded subset of
+    the mixed jobs is compared with the oracle's sieve."""
+    import numpy as np
+
+    chk = Checker()
+    out = {}
+    # the lists gathered so far first, so the host cores start at once
+    timed = [(slice_params(seq[args.warmup + i]), f) for i, f in enumerate(timed_lists)]
+    chk.verify("large_n_timed_slices", timed)
+    if e2e_lists is not None:
+        chk.verify("large_n_host_buffers", [(slice_params(seq[args.warmup + i]), f)
+                                            for i, f in enumerate(e2e_lists)])
+    if mixed is not None:
+        chk.verify("mixed_jobs", list(zip(mixed["jobs"], mixed["lists"])))
+        rng = np.random.default_rng(11)
+        for j in sorted(rng.choice(len(mixed["jobs"]), size=min(16, len(mixed["jobs"])), replace=False)):
+            jp = mixed["jobs"][j]
+            chk.fingerprint("mixed_jobs", jp.pmin, jp.pmax, jp.qmax, int(mixed["job_primes"][j]),
+                            int(mixed["job_sums"][j]))
+    if served is not None:
+        chk.verify("served_jobs", served)
+    full2, out["large_n_full"] = run_full_range(eng, chk, LARGE_N, "large_n_full")
+    _, out["riesel62_full"] = run_full_range(eng, chk, RIESEL62, "riesel62_full")
+    # the timed slices and the host-buffer path gave the same lists as the full run
+    out["large_n_timed_slices"] = {"slices": len(timed_lists), "identical_to_full_run": all(
+        np.array_equal(f, full2[seq[args.warmup + i]]) for i, f in enumerate(timed_lists))}
+    if e2e_lists is not None:
+        out["large_n_host_buffers"] = {"slices": len(e2e_lists), "identical_to_full_run": all(
+            np.array_equal(f, full2[seq[args.warmup + i]]) for i, f in enumerate(e2e_lists))}
+    t0 = time.perf_counter()
+    res = chk.results()
+    for label, r in res.items():
+        out.setdefault(label, {}).update(r)
+    out["checker"] = {"threads": chk.nthreads, "wait_after_gpu_s": time.perf_counter() - t0,
+                      "what": "per line: p prime (deterministic Miller-Rabin), p | k*2^n+c, k and n in "
+                              "the job's ranges with k == koffset (mod kstep), the job's side, no prime "
+                              "factor below 32768; per range: prime count and sum of the oracle's sieve"}
+    return out
 
 
 def run_gpu(args) -> None:
@@ -362,9 +526,11 @@ def run_gpu(args) -> None:
     stats = []
     with Clocks(local) as clk:
         t0 = time.perf_counter()
+        timed_lists = []
         for i in range(args.warmup, need):
-            _, st = eng.run_job(slice_params(seq[i]))
+            fac, st = eng.run_job(slice_params(seq[i]))
             stats.append(st)
+            timed_lists.append(fac)
         barrier()
         elapsed = time.perf_counter() - t0
     launches = eng.launches - launches0
@@ -393,10 +559,12 @@ def run_gpu(args) -> None:
         barrier()
         h2d = d2h = 0
         e_primes = 0
+        e2e_lists = []
         t0 = time.perf_counter()
         for i in range(args.warmup, need):
             jp, pin = host_sets[i]
             fac, st = eng.check_primes(jp, pin.numpy().view(np.uint64))
+            e2e_lists.append(fac)
             h2d += pin.numel() * 8
             d2h += 8 + fac.nbytes
             e_primes += st.primes
@@ -434,9 +602,11 @@ def run_gpu(args) -> None:
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                           "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
     cpu = None if args.no_cpu else cpu_sample(args.ref_seconds)
-    batched = None if args.no_batched else run_mixed(eng, args.mixed_jobs)
-    serving = None if args.no_serving else run_serving(window=args.serve_window)
+    mixed_checked, batched = (None, None) if args.no_batched else run_mixed(eng, args.mixed_jobs)
+    served, serving = (None, None) if args.no_serving else run_serving(window=args.serve_window)
     others = None if args.no_batched else run_other_workloads(eng)
+    verify = None if args.no_verify else run_checks(eng, args, slice_params, seq, timed_lists,
+                                                    e2e_lists if e2e else None, mixed_checked, served)
     line = {"metric": METRIC, "value": value, "unit": "primes/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -453,7 +623,7 @@ def run_gpu(args) -> None:
                          "filter": sum(s.filter_ms for s in stats)},
             "factors": sum(s.factors for s in stats),
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "batched": batched, "serving": serving, "other_workloads": others}
+            "batched": batched, "serving": serving, "other_workloads": others, "verify": verify}
     print(json.dumps(line), flush=True)
     eng.close()
     if ws > 1:
@@ -504,6 +674,8 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-window", type=float, default=4.0)
+    ap.add_argument("--no-verify", action="store_true",
+                    help="skip the checker leg (full-range runs verified by the oracle)")
     ap.add_argument("--mixed-jobs", type=int, default=512)
     ap.add_argument("--profile", type=int, nargs=2, metavar=("SPAN", "NWIDTH"))
     ap.add_argument("--profile-reps", type=int, default=1)

@@ -77,6 +77,12 @@ def load() -> ctypes.CDLL:
         lib.ppo_is_prime.argtypes = [ctypes.c_uint64]
         lib.ppo_kpow_mod.restype = ctypes.c_uint64
         lib.ppo_kpow_mod.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64]
+        lib.ppo_sieve_fingerprint.restype = ctypes.c_int
+        lib.ppo_sieve_fingerprint.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                              ctypes.c_int, P(ctypes.c_uint64), P(ctypes.c_uint64)]
+        lib.ppo_verify_factors.restype = ctypes.c_long
+        lib.ppo_verify_factors.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]
         lib.ppo_sieve_range.restype = ctypes.c_size_t
         lib.ppo_sieve_range.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
                                         P(ctypes.c_uint64), ctypes.c_size_t]
@@ -150,6 +156,41 @@ def sieve_range(lo: int, hi: int, qmax: int) -> np.ndarray:
     out = np.zeros(max(n, 1), dtype=np.uint64)
     lib.ppo_sieve_range(lo, hi, qmax, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n)
     return out[:n]
+
+
+def fingerprint(lo: int, hi: int, qmax: int, nthreads: int | None = None) -> tuple[int, int]:
+    """(count, 64-bit wrapping sum) of the primes in [lo, hi) under the sieve
+    rule with bound qmax: the reference's count=/sum= line for a whole range."""
+    cnt, s = ctypes.c_uint64(), ctypes.c_uint64()
+    load().ppo_sieve_fingerprint(lo, hi, qmax, nthreads or threads(), ctypes.byref(cnt), ctypes.byref(s))
+    return cnt.value, s.value
+
+
+BAD_BITS = {1: "p not prime", 2: "p out of range", 4: "k out of range or residue", 8: "n out of range",
+            16: "wrong side", 32: "p does not divide k*2^n+c", 64: "output rule"}
+
+
+def verify_factors(jobs, factors, job_of=None, nthreads: int | None = None):
+    """Per-line verification of reported factors (kept as the oracle for every
+    run): `jobs` a Params or a list of them, `factors` rows with fields p, k, n,
+    c, `job_of` the job index of each row (None: all rows of jobs[0]).
+    Returns (failures, bad) with bad[i] the failed-check bits of row i."""
+    lib = load()
+    if isinstance(jobs, Params):
+        jobs = [jobs]
+    arr = (Params * len(jobs))(*jobs)
+    f = np.zeros(len(factors), dtype=FACTOR_DTYPE)
+    for name in ("p", "k", "n", "c"):
+        f[name] = factors[name]
+    jo = None
+    if job_of is not None:
+        jo = np.ascontiguousarray(job_of, dtype=np.uint32)
+        assert len(jo) == len(f) and (len(jo) == 0 or int(jo.max()) < len(jobs))
+    bad = np.zeros(len(f), dtype=np.uint8)
+    fails = lib.ppo_verify_factors(ctypes.cast(arr, ctypes.c_void_p),
+                                   jo.ctypes.data if jo is not None else None,
+                                   f.ctypes.data, len(f), nthreads or threads(), bad.ctypes.data)
+    return int(fails), bad
 
 
 def small_factor(k: int, n: int, c: int, qmin: int = 3) -> int:

@@ -576,3 +576,253 @@ long ppo_walk_list(const ppo_params *pp, const uint64_t *P, size_t np, int nthre
   pthread_mutex_destroy(&j.mu);
   return r;
 }
+
+/* ----------------------------------------------------- range fingerprint */
+
+/* The count and 64-bit wrapping sum of the primes a sieve job walks, for
+   ranges far too wide for ppo_sieve_range's output array: the reference's
+   count=/sum= line (main.c:1232) over [lo, hi) with the sieve rule of
+   sieve.c:168-608 (odd p with no prime factor q <= qmax other than p).
+
+   Work items are chunks of up to 2^28 odd candidates, one bit each.  Sieving
+   primes below WIN_BITS are marked window by window (128 KB windows, each q
+   carrying its next multiple from window to window); larger ones first write
+   their multiples' positions into per-window buckets, a bounded group of q at
+   a time, and the buckets are then applied window by window, so that every
+   bit clear lands in a cache-resident window. */
+#define WIN_LOG 20
+#define WIN_BITS ((uint64_t)1 << WIN_LOG)
+#define BUCKET_GROUP_ENTRIES ((size_t)1 << 24)
+
+typedef struct {
+  uint64_t lo;          /* first odd candidate of the range */
+  uint64_t nbits;       /* odd candidates in the range */
+  uint64_t chunk_bits;  /* per work item */
+  uint64_t nchunks;
+  const base_primes *bp;
+  volatile uint64_t next;
+  pthread_mutex_t mu;
+  uint64_t count, sum;
+} fp_job;
+
+typedef struct {
+  uint32_t *e;
+  size_t n, cap;
+} bucket_t;
+
+static void bucket_push(bucket_t *b, uint32_t v)
+{
+  if (b->n == b->cap) {
+    b->cap = b->cap ? 2 * b->cap : 1024;
+    b->e = realloc(b->e, b->cap * sizeof *b->e);
+  }
+  b->e[b->n++] = v;
+}
+
+/* bit index (from chunk value base, odd) of q's first odd multiple that is
+   >= max(q*q, base), or UINT64_MAX when that is beyond hi */
+static uint64_t first_hit(uint64_t q, uint64_t base, uint64_t hi)
+{
+  uint64_t st;
+  if (q * q >= base) {
+    st = q * q;
+  } else {
+    uint64_t r = base % q;
+    st = r ? base + (q - r) : base;
+    if ((st & 1) == 0) st += q;
+  }
+  if (st >= hi) return UINT64_MAX;
+  return (st - base) >> 1;
+}
+
+static void fp_chunk(fp_job *j, uint64_t ci, uint64_t *bits, uint64_t *next_small, bucket_t *bk,
+                     uint64_t *cnt_out, uint64_t *sum_out)
+{
+  const uint64_t b0 = ci * j->chunk_bits;
+  const uint64_t nb = (j->nbits - b0) < j->chunk_bits ? (j->nbits - b0) : j->chunk_bits;
+  const uint64_t base = j->lo + 2 * b0, hi = base + 2 * nb; /* odd values base .. hi-2 */
+  const size_t nw = (size_t)((nb + 63) / 64);
+  memset(bits, 0xff, nw * 8);
+  if (nb & 63) bits[nw - 1] = ((uint64_t)1 << (nb & 63)) - 1;
+  const base_primes *bp = j->bp;
+  /* sieving primes that matter: q*q < hi */
+  size_t nq = 0;
+  while (nq < bp->nq && (uint64_t)bp->q[nq] * bp->q[nq] < hi) nq++;
+  size_t nsmall = 0;
+  while (nsmall < nq && bp->q[nsmall] < WIN_BITS) nsmall++;
+
+  /* small q, window by window */
+  for (size_t t = 0; t < nsmall; t++) next_small[t] = first_hit(bp->q[t], base, hi);
+  for (uint64_t w0 = 0; w0 < nb; w0 += WIN_BITS) {
+    const uint64_t w1 = w0 + WIN_BITS < nb ? w0 + WIN_BITS : nb;
+    for (size_t t = 0; t < nsmall; t++) {
+      const uint64_t q = bp->q[t];
+      uint64_t x = next_small[t];
+      for (; x < w1; x += q) bits[x >> 6] &= ~((uint64_t)1 << (x & 63));
+      next_small[t] = x;
+    }
+  }
+
+  /* large q through per-window buckets, a bounded group at a time */
+  const size_t nwin = (size_t)((nb + WIN_BITS - 1) / WIN_BITS);
+  size_t t = nsmall;
+  while (t < nq) {
+    size_t entries = 0;
+    for (; t < nq && entries < BUCKET_GROUP_ENTRIES; t++) {
+      const uint64_t q = bp->q[t];
+      for (uint64_t x = first_hit(q, base, hi); x < nb; x += q) {
+        bucket_push(&bk[x >> WIN_LOG], (uint32_t)(x & (WIN_BITS - 1)));
+        entries++;
+      }
+    }
+    for (size_t w = 0; w < nwin; w++) {
+      uint64_t *wb = bits + ((uint64_t)w << (WIN_LOG - 6));
+      for (size_t e = 0; e < bk[w].n; e++) {
+        const uint32_t x = bk[w].e[e];
+        wb[x >> 6] &= ~((uint64_t)1 << (x & 63));
+      }
+      bk[w].n = 0;
+    }
+  }
+
+  uint64_t c = 0, s = 0;
+  for (size_t w = 0; w < nw; w++) {
+    uint64_t v = bits[w];
+    while (v) {
+      const int b = __builtin_ctzll(v);
+      v &= v - 1;
+      s += base + 2 * (64 * (uint64_t)w + (uint64_t)b);
+      c++;
+    }
+  }
+  *cnt_out = c;
+  *sum_out = s;
+}
+
+static void *fp_worker(void *arg)
+{
+  fp_job *j = arg;
+  uint64_t *bits = malloc((size_t)((j->chunk_bits + 63) / 64) * 8);
+  uint64_t *next_small = malloc(sizeof(uint64_t) * (size_t)(WIN_BITS / 2 + 16));
+  const size_t nwin = (size_t)((j->chunk_bits + WIN_BITS - 1) / WIN_BITS);
+  bucket_t *bk = calloc(nwin, sizeof *bk);
+  uint64_t c = 0, s = 0;
+  for (;;) {
+    const uint64_t ci = __atomic_fetch_add(&j->next, 1, __ATOMIC_RELAXED);
+    if (ci >= j->nchunks) break;
+    uint64_t cc, ss;
+    fp_chunk(j, ci, bits, next_small, bk, &cc, &ss);
+    c += cc;
+    s += ss;
+  }
+  pthread_mutex_lock(&j->mu);
+  j->count += c;
+  j->sum += s;
+  pthread_mutex_unlock(&j->mu);
+  for (size_t w = 0; w < nwin; w++) free(bk[w].e);
+  free(bk);
+  free(next_small);
+  free(bits);
+  return NULL;
+}
+
+int ppo_sieve_fingerprint(uint64_t lo, uint64_t hi, uint32_t qmax, int nthreads, uint64_t *count,
+                          uint64_t *sum)
+{
+  *count = 0;
+  *sum = 0;
+  lo |= 1;
+  if (lo < 3) lo = 3;
+  if (hi <= lo) return PPO_OK;
+  base_primes bp;
+  get_base_primes(qmax, &bp);
+  fp_job j;
+  memset(&j, 0, sizeof j);
+  pthread_mutex_init(&j.mu, NULL);
+  j.lo = lo;
+  j.nbits = (hi - lo + 1) / 2;
+  j.bp = &bp;
+  if (nthreads < 1) nthreads = 1;
+  /* about four work items per thread, 2^20 .. 2^28 candidates each */
+  uint64_t cb = j.nbits / ((uint64_t)nthreads * 4) + 1;
+  if (cb < WIN_BITS) cb = WIN_BITS;
+  if (cb > ((uint64_t)1 << 28)) cb = (uint64_t)1 << 28;
+  cb = (cb + WIN_BITS - 1) & ~(WIN_BITS - 1);
+  j.chunk_bits = cb;
+  j.nchunks = (j.nbits + cb - 1) / cb;
+  pthread_t *th = malloc((size_t)nthreads * sizeof *th);
+  for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, fp_worker, &j);
+  for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+  free(th);
+  *count = j.count;
+  *sum = j.sum;
+  pthread_mutex_destroy(&j.mu);
+  return PPO_OK;
+}
+
+/* ---------------------------------------------------- per-line verification */
+
+typedef struct {
+  const ppo_params *jobs;
+  const uint32_t *job_of;
+  const ppo_factor *f;
+  size_t n;
+  uint8_t *bad;
+  volatile uint64_t next;
+  volatile long failures;
+} vf_job;
+
+static uint8_t verify_one(const ppo_params *pp, const ppo_factor *x)
+{
+  uint8_t b = 0;
+  if (!ppo_is_prime(x->p)) b |= PPO_BAD_NOT_PRIME;
+  if (x->p < pp->pmin || x->p >= pp->pmax) b |= PPO_BAD_P_RANGE;
+  if (x->k < pp->kmin || x->k > pp->kmax || x->k != pp->kstep * (x->k / pp->kstep) + pp->koffset)
+    b |= PPO_BAD_K;
+  if (x->n < pp->nmin || x->n >= pp->nmax) b |= PPO_BAD_N;
+  if (pp->c == PPO_TWIN ? (x->c != 1 && x->c != -1) : x->c != pp->c) b |= PPO_BAD_C;
+  if ((x->c == 1 || x->c == -1) && x->p > 2 && ppo_kpow_mod(x->k, x->n, x->c, x->p) != 0)
+    b |= PPO_BAD_NOT_DIVISOR;
+  if (!(b & (PPO_BAD_K | PPO_BAD_N | PPO_BAD_C)) && !ppo_test_factor(pp, x->k, x->n, x->c))
+    b |= PPO_BAD_RULE;
+  return b;
+}
+
+static void *vf_worker(void *arg)
+{
+  vf_job *j = arg;
+  const uint64_t B = 64;
+  long bad = 0;
+  for (;;) {
+    const uint64_t i0 = __atomic_fetch_add(&j->next, B, __ATOMIC_RELAXED);
+    if (i0 >= j->n) break;
+    const uint64_t i1 = i0 + B < j->n ? i0 + B : j->n;
+    for (uint64_t i = i0; i < i1; i++) {
+      const ppo_params *pp = &j->jobs[j->job_of ? j->job_of[i] : 0];
+      const uint8_t b = verify_one(pp, &j->f[i]);
+      if (j->bad) j->bad[i] = b;
+      bad += b != 0;
+    }
+  }
+  __atomic_fetch_add(&j->failures, bad, __ATOMIC_RELAXED);
+  return NULL;
+}
+
+long ppo_verify_factors(const ppo_params *jobs, const uint32_t *job_of, const ppo_factor *f, size_t n,
+                        int nthreads, uint8_t *bad)
+{
+  vf_job j;
+  memset(&j, 0, sizeof j);
+  j.jobs = jobs;
+  j.job_of = job_of;
+  j.f = f;
+  j.n = n;
+  j.bad = bad;
+  if (nthreads < 1) nthreads = 1;
+  pthread_once(&g_small_once, init_small_primes);
+  pthread_t *th = malloc((size_t)nthreads * sizeof *th);
+  for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, vf_worker, &j);
+  for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+  free(th);
+  return j.failures;
+}

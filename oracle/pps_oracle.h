@@ -95,6 +95,30 @@ long ppo_run(const ppo_params *pp, int nthreads, ppo_factor *out, size_t cap,
 long ppo_walk_list(const ppo_params *pp, const uint64_t *P, size_t np, int nthreads,
                    ppo_factor *out, size_t cap);
 
+/* Count and 64-bit wrapping sum of the primes in [lo, hi) under the sieve rule
+   (odd p, no prime factor q <= qmax other than p), with nthreads threads: the
+   reference's count=/sum= fingerprint (main.c:1232) of a whole job's range. */
+int ppo_sieve_fingerprint(uint64_t lo, uint64_t hi, uint32_t qmax, int nthreads, uint64_t *count,
+                          uint64_t *sum);
+
+/* Per-line verification of reported factors: line i belongs to
+   jobs[job_of[i]] (jobs[0] when job_of is NULL) and must have p prime
+   (deterministic Miller-Rabin), pmin <= p < pmax, k in [kmin, kmax] with
+   k == koffset (mod kstep), nmin <= n < nmax, c the job's side (+1 or -1 for
+   a twin job), k*2^n + c == 0 (mod p), and pass the job's output rule
+   (ppo_test_factor: pps/app.c:159-186, pps/factor_proth.c:247-253).  bad[i]
+   (optional) receives the PPO_BAD_* bits of the failed checks.  Returns the
+   number of failed lines. */
+#define PPO_BAD_NOT_PRIME 1
+#define PPO_BAD_P_RANGE 2
+#define PPO_BAD_K 4
+#define PPO_BAD_N 8
+#define PPO_BAD_C 16
+#define PPO_BAD_NOT_DIVISOR 32
+#define PPO_BAD_RULE 64
+long ppo_verify_factors(const ppo_params *jobs, const uint32_t *job_of, const ppo_factor *f, size_t n,
+                        int nthreads, uint8_t *bad);
+
 /* Primality (deterministic Miller-Rabin for 64-bit) and k*2^n+c mod p. */
 int ppo_is_prime(uint64_t n);
 uint64_t ppo_kpow_mod(uint64_t k, uint32_t n, int32_t c, uint64_t p);
