@@ -29,15 +29,18 @@ verify : the checker leg, after every timed leg and not timed: the large-n
          line by the oracle on the host cores, and the prime count and sum of
          every full-range slice (and of 16 seeded mixed jobs) are compared with
          the oracle's sieve.
---impl reference: the reference's CPU algorithm (the committed C restatement in
-         oracle/, the reference's own build is not available on the GPU host) on
-         all host cores, one bounded sample of the same workload per step.
+--impl reference: the reference's own CPU path (main.c, sieve.c, pps/app.c,
+         pps/factor_proth.c compiled on this host from the staged reference
+         sources; every prime re-walked by pps/app.c's test_one_p) on all host
+         cores (-t), one bounded sample of the same workload per step; the C
+         restatement in oracle/ where the reference was not built here.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -182,6 +185,59 @@ def cpu_sample(seconds_target: float = 10.0, nthreads: int | None = None) -> dic
             "n_steps_per_sec": count * steps / dt, "seconds": dt, "primes": count}
 
 
+REF_BIN = ROOT / "oracle" / "_ref" / "ppsieve_ref_all"
+FP_RE = re.compile(r"count=(\d+),sum=0x([0-9a-f]+)")
+
+
+def reference_sample(seconds_target: float = 10.0, nthreads: int | None = None,
+                     width: int | None = None) -> dict | None:
+    """Time the reference's OWN CPU path -- its main.c, sieve.c, pps/app.c and
+    pps/factor_proth.c, built on this host from the staged reference sources
+    (oracle/_ref/ppsieve_ref_all: every prime flagged, so the reference's CPU
+    re-walk test_one_p runs over every prime and all n) -- on a bounded p
+    sub-range at the start of the workload's range, with `nthreads` threads
+    (-t).  None where the reference could not be built here."""
+    import tempfile
+
+    if not REF_BIN.exists():
+        return None
+    nthreads = nthreads or (len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count())
+    fixed = width is not None
+    width = width or 2 * 10**6
+    while True:
+        lo = LARGE_N["pmin"]
+        with tempfile.TemporaryDirectory() as td:
+            cmd = [str(REF_BIN), f"-p{lo}", f"-P{lo + width}", "-k1201", "-K9999", "-n2000000", "-N3000000",
+                   f"-t{nthreads}", "-m1024", "-c1000000", "-r1000000", "-q", "-fout.txt"]
+            t0 = time.perf_counter()
+            r = subprocess.run(cmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+            dt = time.perf_counter() - t0
+        m = FP_RE.search(r.stderr)
+        if r.returncode != 0 or not m:
+            return None
+        count = int(m.group(1))
+        if fixed or dt >= seconds_target * 0.5 or width >= 10**9:
+            break
+        width = int(width * min(8.0, max(1.5, seconds_target / max(dt, 1e-3))))
+    steps = (LARGE_N["nmax"] - LARGE_N["nmin"] + 31) // 32
+    return {"value": count / dt, "unit": "primes/s", "cores": nthreads, "kind": "reference",
+            "sample": f"p in [4.2e13, 4.2e13+{width}) = {count} primes, full n range, {dt:.2f} s wall "
+                      f"(process start to exit) with -t{nthreads}; the reference's main.c/sieve.c/pps/app.c "
+                      f"built on this host, every prime re-walked by its CPU path",
+            "n_steps_per_sec": count * steps / dt, "seconds": dt, "primes": count, "width": width}
+
+
+def baseline_sample(seconds_target: float) -> dict:
+    """The CPU baseline: the reference's own CPU path where it was built here,
+    with the restatement's rate beside it; the restatement alone otherwise."""
+    port = cpu_sample(seconds_target)
+    ref = reference_sample(seconds_target)
+    if ref is None:
+        return port
+    ref["port"] = {k: port[k] for k in ("value", "cores", "sample")}
+    return ref
+
+
 def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
     """The mixed-job workload: `count` heterogeneous jobs from `seed`, as plain one-job
     runs (pps_run_job each) and as one batched persistent run (pps_run_batch);
@@ -240,64 +296,109 @@ def run_other_workloads(eng) -> dict:
         dt = time.perf_counter() - t0
         out[name] = {"primes": int(st.primes), "seconds": dt, "primes_per_s": st.primes / dt,
                      "n_steps_per_s": st.steps / dt, "factors": len(fac), "nstep": int(jp.nstep),
-                     "walk_step": int(jp.step), "variant": int(st.variant)}
+                     "walk_step": int(jp.step), "variant": int(st.variant), "split": int(st.split)}
+    # Few primes, long n: p in [4.2e13, 4.2e13 + 1e7) holds about 3.2e5 primes,
+    # about one wave of the GPU's resident threads.  The tuner's threads per
+    # prime against one thread per prime (forced), each timed after a warm-up.
+    jp = ppsgpu.normalize(**dict(LARGE_N, pmax=LARGE_N["pmin"] + 10**7))
+    import numpy as np
+
+    res, lists = {}, {}
+    for label, split in (("split_1", 1), ("tuned", 0)):
+        eng.set_split(split)
+        eng.run_job(jp)
+        t0 = time.perf_counter()
+        fac, st = eng.run_job(jp)
+        dt = time.perf_counter() - t0
+        res[label] = {"split": int(st.split), "seconds": dt, "walk_ms": st.walk_ms,
+                      "n_steps_per_s": st.steps / dt, "walk_steps_per_s": st.steps / (st.walk_ms * 1e-3),
+                      "factors": len(fac)}
+        lists[label] = fac
+    eng.set_split(0)
+    out["large_n_small_range"] = {"p_range": [jp.pmin, jp.pmax], "primes": int(st.primes), **res,
+                                  "speedup": res["split_1"]["seconds"] / res["tuned"]["seconds"],
+                                  "identical_results": bool(np.array_equal(lists["split_1"], lists["tuned"]))}
     return out
 
 
-def run_serving(rates=(10.0, 30.0, 100.0), window: float = 4.0, seed: int = 3) -> dict:
-    """The serving loop: Poisson arrivals at each rate for `window` seconds of
-    jobs from the mixed-job distribution, submitted to the serving loop
-    (pps_server_*); every submitted job is waited for.  Reports per rate the
-    aggregate primes/s (submission of the first job to the last result) and the
-    p50/p99 latency (submission to result ready) of the jobs."""
+def _serve_rate(srv, pool, nxt: int, rng, rate: float, window: float, max_jobs: int, served: list) -> tuple:
+    """Poisson arrivals at `rate` jobs/s for `window` seconds or `max_jobs` jobs,
+    whichever ends first, then every job waited for.  Latency = submission to
+    result ready (the serving loop's own clock)."""
+    import numpy as np
+
+    ids, jps = [], []
+    t0 = time.perf_counter()
+    t = 0.0
+    while len(ids) < max_jobs:
+        t += float(rng.exponential(1.0 / rate))
+        if t > window:
+            break
+        delay = t0 + t - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        jps.append(pool[nxt % len(pool)])
+        ids.append(srv.submit(jps[-1]))
+        nxt += 1
+    submit_s = time.perf_counter() - t0
+    lat, work, primes, factors = [], [], 0, 0
+    for jid, jp in zip(ids, jps):
+        fac, res = srv.wait(jid)
+        served.append((jp, fac))
+        lat.append(res.latency_ms)
+        work.append(res.primes * ((jp.nmax - jp.nmin + jp.step - 1) // jp.step))
+        primes += res.primes
+        factors += len(fac)
+    elapsed = time.perf_counter() - t0
+
+    def rank(v, q):
+        v = sorted(v)
+        return v[max(1, int(np.ceil(q * len(v)))) - 1] if v else None
+
+    # the half of the jobs with the least walk work: what a wave cut bounds
+    # (the largest jobs' latency is mostly their own walk)
+    med = rank(work, 0.5) if work else 0
+    small = [l for l, w in zip(lat, work) if w <= med]
+    return nxt, {"rate_jobs_per_s": rate, "jobs": len(ids), "offered_s": submit_s, "seconds": elapsed,
+                 "achieved_jobs_per_s": len(ids) / elapsed, "primes_per_s": primes / elapsed,
+                 "n_steps_per_s": sum(work) / elapsed, "factors": factors,
+                 "p50_ms": rank(lat, 0.50), "p99_ms": rank(lat, 0.99), "max_ms": max(lat) if lat else None,
+                 "small_half_p50_ms": rank(small, 0.50), "small_half_p99_ms": rank(small, 0.99)}
+
+
+def run_serving(rates=(10.0, 30.0, 100.0, 300.0, 1000.0), window: float = 4.0, max_jobs: int = 400,
+                long_rate: float = 30.0, long_window: float = 60.0, seed: int = 3) -> tuple:
+    """The serving loop (pps_server_*): Poisson arrivals of jobs from the
+    mixed-job distribution at each rate for `window` seconds or `max_jobs`
+    jobs (so the rates above capacity, where a queue builds, still end), then
+    one `long_window`-second window at `long_rate` (below capacity).  Reports
+    per rate the aggregate primes/s and walk steps/s (first submission to last
+    result) and the p50/p99 latency of all jobs and of the smaller half by
+    walk work.  Returns ((job, factors) of every served job, summary)."""
     import numpy as np
 
     import ppsgpu
 
-    need = int(max(rates) * window * 1.3) + 64
+    need = int(sum(min(r * window * 1.3 + 16, max_jobs) for r in rates) + long_rate * long_window * 1.3) + 64
     pool, _ = ppsgpu.mixed_jobs(seed=seed, count=need)
     rng = np.random.default_rng(seed)
-    per_rate = []
-    served = []  # (job, factors) of every job waited for, for the checker
+    per_rate, served = [], []
     with ppsgpu.Server(0) as srv:
         for jp in pool[:8]:  # warm-up: walk tuning, graph capture, sieving primes
             srv.wait(srv.submit(jp))
         nxt = 8
         for rate in rates:
-            ids, jps = [], []
-            t0 = time.perf_counter()
-            t = 0.0
-            while True:
-                t += float(rng.exponential(1.0 / rate))
-                if t > window:
-                    break
-                delay = t0 + t - time.perf_counter()
-                if delay > 0:
-                    time.sleep(delay)
-                jps.append(pool[nxt % len(pool)])
-                ids.append(srv.submit(jps[-1]))
-                nxt += 1
-            lat, primes, factors = [], 0, 0
-            for jid, jp in zip(ids, jps):
-                fac, res = srv.wait(jid)
-                served.append((jp, fac))
-                lat.append(res.latency_ms)
-                primes += res.primes
-                factors += len(fac)
-            elapsed = time.perf_counter() - t0
-            lat_sorted = sorted(lat)
-
-            def rank(q):
-                return lat_sorted[max(1, int(np.ceil(q * len(lat_sorted)))) - 1] if lat_sorted else None
-
-            per_rate.append({"rate_jobs_per_s": rate, "jobs": len(ids), "seconds": elapsed,
-                             "primes_per_s": primes / elapsed, "factors": factors,
-                             "p50_ms": rank(0.50), "p99_ms": rank(0.99)})
+            nxt, r = _serve_rate(srv, pool, nxt, rng, rate, window, max_jobs, served)
+            per_rate.append(r)
+        long = None
+        if long_window > 0:
+            nxt, long = _serve_rate(srv, pool, nxt, rng, long_rate, long_window, 1 << 30, served)
         st = srv.stats()
-    return served, {"workload": f"Poisson arrivals, {window:g} s per rate, jobs of the mixed-job "
-                        f"distribution (seed {seed})",
-            "rates": per_rate, "waves": int(st.waves), "busy_ms": st.busy_ms,
-            "completed": int(st.completed), "failed": int(st.failed)}
+    return served, {"workload": f"Poisson arrivals, {window:g} s or {max_jobs} jobs per rate, then "
+                                f"{long_window:g} s at {long_rate:g} jobs/s; jobs of the mixed-job distribution "
+                                f"(seed {seed}); waves cut at 4e10 walk steps",
+                    "rates": per_rate, "long_window": long, "waves": int(st.waves), "busy_ms": st.busy_ms,
+                    "completed": int(st.completed), "failed": int(st.failed)}
 
 
 RIESEL62 = dict(pmin=(1 << 62) - (1 << 34), pmax=1 << 62, kmin=3, kmax=9999, nmin=100000, nmax=1000000,
@@ -411,8 +512,16 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     per_step = []
+    # each step one bounded sample, sized once so that the whole run stays
+    # within a few minutes
+    target = min(args.ref_seconds, 150.0 / (args.warmup + args.steps))
+    width = None
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(seconds_target=args.ref_seconds)
+        r = reference_sample(seconds_target=target, width=width)
+        if r is None:
+            r = cpu_sample(seconds_target=target)
+        else:
+            width = r["width"]
         if i >= args.warmup:
             per_step.append(r)
     value = statistics.median(r["value"] for r in per_step)
@@ -424,7 +533,7 @@ def run_reference(args) -> None:
             "data": "synthetic (deterministic p range of the configuration)",
             "config": {"workload": WORKLOAD, "sample": last["sample"]},
             "cpu_baseline": {"value": value, "unit": "primes/s", "cores": last["cores"],
-                             "kind": "port", "sample": last["sample"]},
+                             "kind": last["kind"], "sample": last["sample"]},
             "e2e": {"value": value, "unit": "primes/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "n_steps_per_sec": statistics.median(r["n_steps_per_sec"] for r in per_step)}
@@ -601,9 +710,10 @@ def run_gpu(args) -> None:
                           "frac": (sieve_gbs / hbm) if (sieve_gbs and hbm) else None,
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                           "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
-    cpu = None if args.no_cpu else cpu_sample(args.ref_seconds)
+    cpu = None if args.no_cpu else baseline_sample(args.ref_seconds)
     mixed_checked, batched = (None, None) if args.no_batched else run_mixed(eng, args.mixed_jobs)
-    served, serving = (None, None) if args.no_serving else run_serving(window=args.serve_window)
+    served, serving = (None, None) if args.no_serving else run_serving(window=args.serve_window,
+                                                                       long_window=args.serve_long)
     others = None if args.no_batched else run_other_workloads(eng)
     verify = None if args.no_verify else run_checks(eng, args, slice_params, seq, timed_lists,
                                                     e2e_lists if e2e else None, mixed_checked, served)
@@ -674,6 +784,8 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-window", type=float, default=4.0)
+    ap.add_argument("--serve-long", type=float, default=60.0,
+                    help="seconds of the long serving window at 30 jobs/s (0: none)")
     ap.add_argument("--no-verify", action="store_true",
                     help="skip the checker leg (full-range runs verified by the oracle)")
     ap.add_argument("--mixed-jobs", type=int, default=512)

@@ -106,6 +106,8 @@ typedef struct {
   uint32_t batches;     /* device batches used */
   uint32_t variant;     /* walk kernel variant used */
   double   sieve_ms, walk_ms, filter_ms, total_ms;  /* device time per phase */
+  uint32_t split;       /* threads per prime of the walk (the tuner's choice, 1..8) */
+  uint32_t reserved;
 } pps_job_stats;
 
 typedef struct pps_engine pps_engine;
@@ -147,6 +149,14 @@ int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 /* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
 #define PPS_NUM_VARIANTS 26
 int pps_engine_set_variant(pps_engine *e, int variant);
+
+/* Force the threads per prime of the queued walks (1, 2, 4 or 8: each prime's
+   n range is cut into that many parts walked side by side), or 0 for the
+   tuner's choice (timed per job size where a job has fewer primes than a few
+   waves of resident threads).  In the batched form and the serving loop the
+   same number of n parts is used for every job (tuned: long n ranges are cut
+   into parts of about the tuned work per chunk). */
+int pps_engine_set_split(pps_engine *e, int split);
 
 /* Whole job: device sieve of [pmin,pmax), walk, filter.  Factors are sorted by
    (p, k, n); *nout is the total found (may exceed cap -> PPS_ERR_OVERFLOW, with
@@ -264,6 +274,10 @@ typedef struct {
   uint64_t factor_bytes;   /* candidate-buffer budget; 0 = 1 GiB */
   uint32_t max_jobs;       /* admitted jobs at once (device slots); 0 = 4096, at most 65536 */
   uint32_t wave_segments;  /* sieve segments (2^18 odd candidates) per wave; 0 = the maximum, 16384 */
+  uint64_t wave_work;      /* walk steps per wave, estimated from each piece's p range and n
+                              range (primes ~ width / ln p); 0 = 4e10 (about 15 ms of the
+                              GPU); a piece is at least one segment.  A job that arrives
+                              while a wave runs joins the next one, so this bounds its wait. */
 } pps_server_config;
 
 #define PPS_JOB_QUEUED  0  /* submitted, waiting for admission */

@@ -10,6 +10,12 @@
    examine the whole [nmin, nmax) range of every flagged prime.  Nothing here is
    part of the shipped library.
 
+   With -DPPS_STUB_FLAG_ALL every prime is flagged, so that the reference's own
+   CPU re-walk runs over every prime and the stand-in does no walking of its
+   own: the reference's CPU path as a timed baseline (each prime without a
+   candidate makes the re-walk print "Computation Error: no candidates found"
+   on stderr, pps/app.c:1116-1120).
+
    Parameter handling restates pps/appcu.cu:155-209 (cuda_init): nstep clamp to
    nmax-nmin+1, the 2^(64-nstep) <= pmin requirement, forcing nstep to 32 when
    32 <= nstep < 48 and pmin >= 2^32, and the r0 / bbits constants that
@@ -132,7 +138,7 @@ void get_factors_found(unsigned char *factor_found, const unsigned int cthread_c
                        const uint64_t start_t, int *check_ns_delay)
 {
   (void)start_t; (void)check_ns_delay;
-#ifdef SEARCH_TWIN
+#if defined(SEARCH_TWIN) || defined(PPS_STUB_FLAG_ALL)
   memset(factor_found, 1, cthread_count);
 #else
   for (unsigned int i = 0; i < cthread_count; i++)

@@ -53,6 +53,11 @@ struct BJob {
   uint32_t bound_hi;
   // sw_mask != 0: walk form 1 with test 4 (the window K < 2^s read off the step)
   uint32_t sw_mask;
+  // n parts per prime (1, 2, 4, 8): each chunk of primes is walked as nsplit
+  // work items, item j holding blocks [j L, (j+1) L) of the n range,
+  // L = ceil(blocks / nsplit), so a long-n job's work comes in pieces of
+  // about the same size as a short-n job's
+  uint32_t nsplit;
 };
 
 struct BBatch {
@@ -261,6 +266,18 @@ __global__ void k_bsieve_large(const uint8_t* tables, const uint32_t* q, const u
   }
 }
 
+// All bits set in the segments of this wave only (the large-prime scatter
+// clears bits in them next); a wave of few segments does not pay for the
+// whole 512 MB bitmap.
+__global__ void k_bclear(const uint8_t* tables, uint32_t* bitmap) {
+  const uint64_t words = (uint64_t)wt(tables)->nseg * SEG_WORDS;
+  uint4* b4 = (uint4*)bitmap;
+  const uint4 ones = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words / 4;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    b4[i] = ones;
+}
+
 __global__ void __launch_bounds__(SIEVE_THREADS) k_bsieve_seg(const uint8_t* tables, const uint32_t* q,
                                                               uint32_t* bitmap, uint32_t* seg_count) {
   __shared__ uint32_t sb[SEG_WORDS];
@@ -406,8 +423,8 @@ __global__ void k_bchunks(const uint8_t* tables, const BJob* jobs, const uint32_
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < WAVE_SEGS; s += gridDim.x * blockDim.x) {
     uint32_t n = 0;
     if (s < T->nseg) {
-      const uint32_t chunk = jobs[T->batch[T->seg[s].batch].job].chunk;
-      n = (seg_count[s] + chunk - 1) / chunk;
+      const BJob& J = jobs[T->batch[T->seg[s].batch].job];
+      n = (seg_count[s] + J.chunk - 1) / J.chunk * J.nsplit;
     }
     chunk_count[s] = n;
   }
@@ -501,20 +518,26 @@ __device__ __forceinline__ uint32_t b_pinv(uint64_t ps, uint32_t s) {
 //   3  the window with win_u == 0 (test 0 without the shift);
 //   4  walk form 1: K < 2^s, i.e. the step's own high word K >> s is zero,
 //      or the low s+1-kb bits of K zero (sw_mask).
+// `part` (< J.nsplit) is the part of the n range this round walks: blocks
+// [b_lo, b_hi) and, in the last part, the partial last block.
 template <int FORM, int U, int TEST, bool TW>
-__device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p, uint64_t ps, bool valid,
-                                        uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk, pps_hit* hits,
-                                        uint32_t* hit_count, uint32_t hit_cap) {
+__device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint32_t part, uint64_t p, uint64_t ps,
+                                        bool valid, uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk,
+                                        pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t s = FORM == 0 ? 32u : J.step;
   const uint32_t nsteps = J.nsteps, full = nsteps / (uint32_t)U;
+  const uint32_t nsplit = J.nsplit > 1u ? J.nsplit : 1u;
+  const uint32_t per = (full + nsplit - 1u) / nsplit;
+  const uint32_t b_lo = min(full, part * per), b_hi = min(full, b_lo + per);
+  const bool last_part = part == nsplit - 1u;
   const uint32_t tag = job | (J.proth == 1u ? SIDE_PROTH : 0u);  // the walked value's side
   qp[lane] = p;
   if (valid) {
     uint32_t pa, pb;
     b_words<FORM>(p, &pa, &pb);
     const uint32_t pinv_s = b_pinv<FORM>(ps, s);
-    const uint64_t x = inv_pow2(J.nmin, p, ps);
+    const uint64_t x = inv_pow2(J.nmin + s * (uint32_t)U * b_lo, p, ps);
     const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
     const uint32_t win_hi = J.win_hi, win_mask = J.win_mask, win_sh = J.win_sh, win_u = J.win_u;
@@ -530,7 +553,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
       tw_above = (lim != 0ull && p > lim) ? p - lim : 0ull;
       tw_low = lo32(p) & win_mask;
     }
-    for (uint32_t b = 0; b < full; ++b) {
+    for (uint32_t b = b_lo; b < b_hi; ++b) {
       bool f = false;
       uint32_t acc = 0xffffffffu;
 #pragma unroll
@@ -558,7 +581,7 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
         if (pos < BQ_CAP) qe[pos] = (lane << 27) | b;
       }
     }
-    if (full * (uint32_t)U < nsteps) {
+    if (last_part && full * (uint32_t)U < nsteps) {
       // the partial last block: its start value is at hand, keep it
       qk[lane] = mk64(klo, khi);
       const uint32_t pos = atomicAdd(qc, 1u);
@@ -598,14 +621,16 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint64_t p,
       }
     }
   } else if (valid) {
+    // queue overflow: the exact test at every step of this part
     uint32_t pa, pb;
     b_words<FORM>(p, &pa, &pb);
     const uint32_t pinv_s = b_pinv<FORM>(ps, s);
-    const uint64_t x = inv_pow2(J.nmin, p, ps);
+    const uint32_t t_lo = (uint32_t)U * b_lo, t_hi = last_part ? nsteps : (uint32_t)U * b_hi;
+    const uint64_t x = inv_pow2(J.nmin + s * t_lo, p, ps);
     const uint64_t K = J.proth == 1u ? p - x : x;
     uint32_t klo = lo32(K), khi = hi32(K);
 #pragma unroll 1
-    for (uint32_t t = 0; t < nsteps; ++t) {
+    for (uint32_t t = t_lo; t < t_hi; ++t) {
       b_record(klo, khi, J.nmin + s * t, s, p, tag, J, hits, hit_count, hit_cap);
       if (TW) {
         const uint64_t v = p - mk64(klo, khi);
@@ -644,7 +669,11 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
     const uint32_t s = chunk_seg[c];
     const uint32_t job = T->batch[T->seg[s].batch].job;
     const BJob J = jobs[job];
-    const uint32_t within = (uint32_t)(c - chunk_off[s]) * J.chunk;
+    // work items of a segment: its chunks of primes, each as nsplit n parts
+    const uint32_t w = (uint32_t)(c - chunk_off[s]);
+    const uint32_t nsplit = J.nsplit > 1u ? J.nsplit : 1u;
+    const uint32_t part = w % nsplit;
+    const uint32_t within = (w / nsplit) * J.chunk;
     const uint32_t count = min(J.chunk, seg_count[s] - within);
     const uint64_t first = (uint64_t)seg_off[s] + within;
     for (uint32_t r = 0; r < count; r += 32u) {
@@ -652,8 +681,8 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
       const uint64_t pi = first + r + (valid ? lane : 0u);
       const uint64_t p = P[pi], ps = Pinv[pi];
 #define PPS_BROUND(FORM_, TEST_, TW_)                                                                    \
-  b_round<FORM_, U, TEST_, TW_>(J, job, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], hits, \
-                                hit_count, hit_cap)
+  b_round<FORM_, U, TEST_, TW_>(J, job, part, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], \
+                                hits, hit_count, hit_cap)
 #define PPS_BROUND_F(FORM_)                                                                             \
   do {                                                                                                  \
     if (wsh) {                                                                                          \
@@ -741,8 +770,9 @@ int ensure_state(pps_engine* e) {
     // p > 2^32: odd primes are fewer than 1/10 of the odd candidates
     b->prime_cap = (uint64_t)WAVE_SEGS * SEG_BITS / 10 + 4096;
     if ((rc = b->P.ensure(b->prime_cap)) || (rc = b->Pinv.ensure(b->prime_cap))) return rc;
-    // at most prime_cap/32 + one partial chunk per segment (smallest chunk: 32)
-    if ((rc = b->chunk_seg.ensure(b->prime_cap / 32 + WAVE_SEGS))) return rc;
+    // at most prime_cap/32 + one partial chunk per segment (smallest chunk: 32),
+    // each as up to 8 n parts
+    if ((rc = b->chunk_seg.ensure(8 * (b->prime_cap / 32 + WAVE_SEGS)))) return rc;
     if ((rc = b->tot.ensure(8))) return rc;
     if ((rc = b->counters.ensure(4))) return rc;
     if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
@@ -764,14 +794,14 @@ int ensure_state(pps_engine* e) {
   return PPS_OK;
 }
 
-constexpr uint64_t WAVE_KERNELS = 10;  // kernels in one wave's launch sequence
+constexpr uint64_t WAVE_KERNELS = 11;  // kernels in one wave's launch sequence
 
 // The fixed per-wave launch sequence (everything reads counts from the tables).
 int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, uint64_t chunk_limit,
                 pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
   BatchState* b = e->batch;
   cudaStream_t st = e->st;
-  CU(cudaMemsetAsync(b->bitmap.p, 0xff, (size_t)WAVE_SEGS * SEG_WORDS * 4, st));
+  k_bclear<<<e->num_sms * 8, 256, 0, st>>>(b->tables.p, b->bitmap.p);
   CU(cudaMemsetAsync(b->tot.p, 0, 8 * sizeof(uint64_t), st));
   k_bcounts<<<(WAVE_BATCHES + 255) / 256, 256, 0, st>>>(b->tables.p, dq, nq_all, b->large_items.p);
   k_bscan<<<1, 1024, 0, st>>>(b->large_items.p, b->large_off.p, WAVE_BATCHES, b->tot.p + 4);
@@ -831,6 +861,7 @@ BJob make_job(const pps_job_params& jp) {
   J.qmax = jp.qmax;
   J.sign = jp.sign;
   J.chunk = 32;
+  J.nsplit = 1;
   J.win_u = a.win_hi == 0xffffffffu ? 32u : (uint32_t)__builtin_popcount(a.win_hi);
   J.bound_hi = 0xffffffffu;
   if (jp.step == 32 && jp.kmax < (1ull << 32) && jp.pmin / jp.kmax >= (1ull << 43)) J.bound_hi = a.bound_hi;
@@ -867,12 +898,21 @@ BJob make_job(const pps_job_params& jp) {
   return J;
 }
 
-// Each job's chunk holds about `work` walk steps per lane, so a chunk of a
-// short-n job and one of a long-n job take about the same time.
-uint32_t chunk_for(const BJob& J, int work) {
-  const uint64_t per = std::max<uint64_t>(1, J.nsteps);
+// Each job's work item holds about `work` walk steps per lane, so an item of
+// a short-n job and one of a long-n job take about the same time: a long n
+// range is cut into up to 8 parts (n-chunks of at least 32 blocks of 16 steps,
+// and at most 8 times `work` steps where a cut is possible), and a chunk holds
+// `work` x 32 / (steps per part) primes (at least 32: one per lane).
+// A forced split (pps_engine_set_split) replaces the choice for every job.
+void chunk_for(BJob* J, int work, int forced_split) {
+  const uint64_t nsteps = std::max<uint64_t>(1, J->nsteps);
+  uint32_t t = 1;
+  while (t < 8 && nsteps / t > 8ull * (uint64_t)work && nsteps / (2ull * t) >= 32ull * 16ull) t *= 2;
+  if (forced_split > 0) t = (uint32_t)forced_split;
+  const uint64_t per = (nsteps + t - 1) / t;
   const uint64_t c = ((uint64_t)work * 32u / per + 31u) & ~31ull;
-  return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 32), MAX_CHUNK);
+  J->nsplit = t;
+  J->chunk = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 32), MAX_CHUNK);
 }
 
 // Copy mirror slots [lo, hi) to the device.  The source is pageable: the call
@@ -891,9 +931,11 @@ int set_chunks(pps_engine* e, uint32_t lo, uint32_t hi, int work) {
   bool changed = false;
   for (uint32_t s = lo; s <= hi; ++s) {
     if (!b->slot_pmax[s]) continue;
-    const uint32_t c = chunk_for(b->hjobs[s], work);
-    if (c != b->hjobs[s].chunk) {
-      b->hjobs[s].chunk = c;
+    BJob J = b->hjobs[s];
+    chunk_for(&J, work, e->forced_split);
+    if (J.chunk != b->hjobs[s].chunk || J.nsplit != b->hjobs[s].nsplit) {
+      b->hjobs[s].chunk = J.chunk;
+      b->hjobs[s].nsplit = J.nsplit;
       changed = true;
     }
   }
@@ -939,7 +981,7 @@ int batch_set_jobs(pps_engine* e, uint32_t slot0, const pps_job_params* jobs, si
   const int work = b->tuned_work > 0 ? b->tuned_work : 1024;
   for (size_t j = 0; j < n; ++j) {
     BJob J = make_job(jobs[j]);
-    J.chunk = chunk_for(J, work);
+    chunk_for(&J, work, e->forced_split);
     b->hjobs[slot0 + j] = J;
     b->slot_pmax[slot0 + j] = jobs[j].pmax;
   }
@@ -1081,12 +1123,14 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
         CU(cudaEventSynchronize(e->ev[1]));
         float ms = 0;
         CU(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
-        // steps timed: the chunks walked (the wave may hold fewer than lim), each
-        // with the chunk size of the wave's first job, whose primes come first
+        // steps timed: the work items walked (the wave may hold fewer than lim),
+        // each with the chunk size and n part of the wave's first job, whose
+        // primes come first
         uint64_t nch = 0;
         CU(cudaMemcpy(&nch, b->tot.p + 2, sizeof nch, cudaMemcpyDeviceToHost));
         const BJob& J0 = b->hjobs[T->batch[0].job];
-        const double steps = (double)std::min<uint64_t>(lim, nch) * J0.chunk * std::max<uint32_t>(J0.nsteps, 1);
+        const double part_steps = (double)std::max<uint32_t>(J0.nsteps, 1) / std::max<uint32_t>(J0.nsplit, 1);
+        const double steps = (double)std::min<uint64_t>(lim, nch) * J0.chunk * part_steps;
         const float per_step = (float)(ms / std::max(steps, 1.0));
         if (per_step < best) {
           best = per_step;

@@ -243,6 +243,13 @@ extern "C" int pps_engine_set_variant(pps_engine* e, int v) {
   return PPS_OK;
 }
 
+extern "C" int pps_engine_set_split(pps_engine* e, int split) {
+  if (!e || (split != 0 && split != 1 && split != 2 && split != 4 && split != 8))
+    return set_err(PPS_ERR_INVALID_PARAM, "bad split %d (0, 1, 2, 4 or 8)", split);
+  e->forced_split = split;
+  return PPS_OK;
+}
+
 extern "C" uint64_t pps_engine_launches(const pps_engine* e) { return e ? e->launches : 0; }
 
 // ----------------------------------------------------------------- sieve
@@ -466,10 +473,13 @@ static int variant_ok(const pps_job_params* jp, int v) {
 }
 
 static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64_t* dP, const uint64_t* dPinv,
-                    const uint64_t* d_np, uint64_t np_max, uint32_t idx_base, uint32_t nsteps_cap) {
+                    const uint64_t* d_np, uint64_t np_max, uint32_t idx_base, uint32_t nsteps_cap,
+                    uint32_t split = 1) {
   WalkArgs a;
   fill_walk_args(jp, &a);
   if (nsteps_cap && a.nsteps > nsteps_cap) a.nsteps = nsteps_cap;
+  // threads per prime: queued walks only (variants 10 and up)
+  a.nsplit = v >= 10 && split > 1 ? split : 1;
   a.P = dP;
   a.Pinv = dPinv;
   a.d_np = d_np;
@@ -481,7 +491,8 @@ static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64
   const int threads = 256;
   int maxb = walk_max_blocks(v, threads, jp->step, e->num_sms);
   if (maxb <= 0) return set_err(PPS_ERR_CUDA, "walk variant %d unavailable", v);
-  uint64_t need = (np_max + threads - 1) / threads;
+  const uint64_t nvirt = v >= 10 ? ((np_max + 31) & ~31ull) * a.nsplit : np_max;
+  uint64_t need = (nvirt + threads - 1) / threads;
   // The queued walks (variants 10 and up) get one thread per prime: the block
   // scheduler then hands new primes to whichever SM has finished its blocks, so
   // every SM keeps its full complement of warps to the end (with a grid of one
@@ -538,6 +549,22 @@ static double pretest_pass_rate(const pps_job_params* jp, int v) {
   return std::min(r, 1.0);
 }
 
+// The walk variants the tuner may pick for a job (bit v: variant v): those
+// exact for it whose pre-test passes at most 1 step in 512 and, for the queued
+// walks, whose expected queue load over the whole n range fits in half the
+// warp queue; every exact variant where none does.
+static uint32_t variant_set(const pps_job_params* jp) {
+  const double nsteps_full = jp->nmax > jp->nmin ? (double)((jp->nmax - jp->nmin + jp->step - 1) / jp->step) : 0.0;
+  uint32_t exact = 0, cls = 0;
+  for (int v = 0; v < PPS_NUM_VARIANTS; ++v)
+    if (variant_ok(jp, v)) {
+      exact |= 1u << v;
+      const double r = pretest_pass_rate(jp, v);
+      if (r <= 1.0 / 512.0 && (v < 10 || 32.0 * nsteps_full * r <= WALK_QUEUE_CAP / 2)) cls |= 1u << v;
+    }
+  return cls ? cls : exact;
+}
+
 // Time each walk variant on the first `np` resident primes with a capped n
 // range and keep the fastest for this step class.
 static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP, const uint64_t* dPinv,
@@ -551,15 +578,7 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   // overflows on the full range (each lane then re-walks its prime exactly);
   // and without the rate bound a choice timed on one job could be reused for a
   // job of the same kind at much smaller p, where its window passes most steps.
-  const double nsteps_full = jp->nmax > jp->nmin ? (double)((jp->nmax - jp->nmin + jp->step - 1) / jp->step) : 0.0;
-  uint32_t exact = 0, cls = 0;
-  for (int v = 0; v < PPS_NUM_VARIANTS; ++v)
-    if (variant_ok(jp, v)) {
-      exact |= 1u << v;
-      const double r = pretest_pass_rate(jp, v);
-      if (r <= 1.0 / 512.0 && (v < 10 || 32.0 * nsteps_full * r <= WALK_QUEUE_CAP / 2)) cls |= 1u << v;
-    }
-  if (!cls) cls = exact;
+  const uint32_t cls = variant_set(jp);
   // jobs are told apart by that set (step size, side, window kind, bound test,
   // pass rates): a choice is reused only within the same set
   // a forced variant is honoured only where it is exact for this job
@@ -613,6 +632,62 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   if (slot == e->tuned_variant.size()) e->tuned_variant.push_back({});
   e->tuned_variant[slot] = {cls, best, work};
   return best;
+}
+
+static int ceil_lg(uint64_t x) {
+  int r = 0;
+  while ((1ull << r) < x && r < 63) r++;
+  return r;
+}
+
+// Threads per prime for the queued walk v on np primes (1 where the walk is not
+// a queued one).  Where the job's primes fill fewer than four waves of resident
+// threads, the last wave leaves SMs idle; cutting each prime's n range into T
+// parts fills them, at the cost of one more start value (an exponentiation) per
+// part.  T in {1, 2, 4, 8} (parts of at least 32 blocks) is timed on the job's
+// own primes with the same total steps for every T, and the choice is kept per
+// (variant set, variant, log2 primes, log2 steps).
+static int choose_split(pps_engine* e, const pps_job_params* jp, uint32_t cls, int v, const uint64_t* dP,
+                        const uint64_t* dPinv, uint64_t np) {
+  if (v < 10 || np == 0) return 1;
+  if (e->forced_split > 0) return e->forced_split;
+  WalkArgs a;
+  fill_walk_args(jp, &a);
+  const uint32_t U = (v == 13 || v == 14) ? 16u : 8u;
+  const uint32_t blocks = a.nsteps / U;
+  const uint64_t resident = (uint64_t)walk_max_blocks(v, 256, jp->step, e->num_sms) * 256;
+  if (resident == 0 || np >= 4 * resident || blocks < 64) return 1;
+  const int lg_np = ceil_lg(np), lg_steps = ceil_lg(a.nsteps);
+  for (const auto& t : e->tuned_split)
+    if (t.mask == cls && t.variant == v && t.lg_np == lg_np && t.lg_steps == lg_steps) return (int)t.split;
+  // the same total steps for every T (at most 16384 per prime), so that
+  // only the wave fill and the per-part start values differ
+  const uint32_t cap = std::min<uint32_t>(a.nsteps, 16384);
+  uint32_t best = 1;
+  float best_ms = 1e30f;
+  for (uint32_t T = 1; T <= 8; T *= 2) {
+    if (T > 1 && cap / U < 32 * T) break;
+    int rc;
+    CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
+    if ((rc = run_walk(e, jp, v, dP, dPinv, nullptr, np, 0, cap, T))) return rc;  // warm-up
+    CU(cudaEventRecord(e->ev[6], e->st));
+    for (int r = 0; r < 2; ++r)
+      if ((rc = run_walk(e, jp, v, dP, dPinv, nullptr, np, 0, cap, T))) return rc;
+    CU(cudaEventRecord(e->ev[7], e->st));
+    CU(cudaEventSynchronize(e->ev[7]));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
+    if (tune_log())
+      fprintf(stderr, "pps tune: variant %d, %llu primes, %u steps: split %u %.3f ms\n", v,
+              (unsigned long long)np, cap, T, ms);
+    if (ms < best_ms * 0.97f) {  // a larger T must win clearly
+      best_ms = ms;
+      best = T;
+    }
+  }
+  CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
+  e->tuned_split.push_back({cls, v, lg_np, lg_steps, best});
+  return (int)best;
 }
 
 static int ensure_hit_buffers(pps_engine* e, size_t hit_cap, size_t fac_cap) {
@@ -751,8 +826,11 @@ static int run_job_once(pps_engine* e, const pps_job_params* jp, pps_factor* out
       if (variant < 0) return variant;
       if (st) st->variant = (uint32_t)variant;
     }
+    const int split = choose_split(e, jp, variant_set(jp), variant, e->P.p, e->Pinv.p, np);
+    if (split < 0) return split;
+    if (st) st->split = std::max<uint32_t>(st->split, (uint32_t)split);
     CU(cudaEventRecord(e->ev[2], e->st));
-    if ((rc = run_walk(e, jp, variant, e->P.p, e->Pinv.p, nullptr, np, 0, 0))) return rc;
+    if ((rc = run_walk(e, jp, variant, e->P.p, e->Pinv.p, nullptr, np, 0, 0, (uint32_t)split))) return rc;
     CU(cudaEventRecord(e->ev[3], e->st));
     if (st) {
       CU(cudaEventSynchronize(e->ev[3]));
@@ -830,8 +908,11 @@ static int walk_device_list(pps_engine* e, const pps_job_params* jp, const uint6
   int variant = autotune(e, jp, dP, nullptr, np);
   if (variant < 0) return variant;
   if (st) st->variant = (uint32_t)variant;
+  const int split = choose_split(e, jp, variant_set(jp), variant, dP, nullptr, np);
+  if (split < 0) return split;
+  if (st) st->split = (uint32_t)split;
   CU(cudaEventRecord(e->ev[2], e->st));
-  int rc = run_walk(e, jp, variant, dP, nullptr, nullptr, np, 0, 0);
+  int rc = run_walk(e, jp, variant, dP, nullptr, nullptr, np, 0, 0, (uint32_t)split);
   if (rc) return rc;
   CU(cudaEventRecord(e->ev[3], e->st));
   if (st) {

@@ -75,6 +75,16 @@ struct pps_engine {
     uint64_t work;
   };
   std::vector<Tuned> tuned_variant;
+  // threads per prime of the queued walks: forced (0: tuned), and the tuned
+  // choice per (variant set, variant, log2 primes, log2 steps)
+  int forced_split = 0;
+  struct TunedSplit {
+    uint32_t mask;
+    int variant;
+    int lg_np, lg_steps;
+    uint32_t split;
+  };
+  std::vector<TunedSplit> tuned_split;
   uint64_t launches = 0;
 
   // sieving primes (ascending odd primes <= base_limit), u32

@@ -57,6 +57,9 @@ struct WalkArgs {
   uint32_t shift_ok;        // step < 32 and pmax <= 2^(32+step): the shifted chain step
   uint32_t sw_mask;         // steps s < 32: K < 2^s (hi word of K 2^(32-s) zero) or (lo & sw_mask) == 0,
                             // sw_mask = 2^(s+1-kb) - 1 (0 where s < kb)
+  uint32_t nsplit;          // queued walks: threads per prime (1, 2, 4, 8): thread j of a
+                            // prime walks blocks [j L, (j+1) L) of its n range,
+                            // L = ceil(blocks / nsplit); 0 counts as 1
   uint32_t idx_base;        // added to the prime index in hit records
   pps_hit* hits;
   uint32_t* hit_count;      // may exceed hit_cap: overflow is detected by host

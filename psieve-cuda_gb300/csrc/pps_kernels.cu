@@ -360,6 +360,16 @@ __global__ void __launch_bounds__(256) k_walk(WalkArgs a) {
 // warp's primes finish their walk, the warp re-checks the queued blocks together
 // (one block per lane), recomputing each block's starting value as
 // -/+2^-(nmin + 32 U b) mod p.  The hot loop thus holds no exact-check code.
+//
+// Threads per prime (a.nsplit = T): the n range's blocks are cut into T parts
+// of L = ceil(blocks / T) blocks, and part j of every prime is walked by its
+// own thread, starting from -/+2^-(nmin + s U j L) mod p (the same start value
+// the queue re-check computes).  Virtual threads are numbered part-major over
+// the prime count rounded up to 32, so each warp holds 32 consecutive primes
+// of one part (every lane runs the same number of blocks).  A job with fewer
+// primes than the GPU holds threads then still fills every SM (the
+// reference's per-launch n slices, pps/appcu.cu:337-357, split n the same way
+// but across launches).
 constexpr int WQ_CAP = WALK_QUEUE_CAP;   // queue entries per warp
 constexpr int WQ_WARPS = 8;   // warps per 256-thread block
 
@@ -430,20 +440,30 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
   const uint32_t s = FORM == 0 ? 32u : a.step, sh = 32u - s;
   const uint32_t nsteps = a.nsteps, nmin = a.nmin;
   const uint32_t full = nsteps / (uint32_t)U;  // whole blocks of U steps
+  const uint32_t nsplit = a.nsplit > 1u ? a.nsplit : 1u;
+  const uint32_t part = (full + nsplit - 1u) / nsplit;  // blocks per part
+  const uint64_t npad = (np + 31ull) & ~31ull;
+  const uint64_t nvirt = npad * nsplit;
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const uint64_t wstride = (uint64_t)gridDim.x * blockDim.x;
   if (lane == 0) q_cnt[wib] = 0;
   __syncwarp();
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < np;
-       base += wstride) {
+  for (uint64_t vbase = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); vbase < nvirt;
+       vbase += wstride) {
+    const uint32_t j = nsplit > 1u ? (uint32_t)(vbase / npad) : 0u;  // the part, warp-uniform
+    const uint64_t base = vbase - (uint64_t)j * npad;                // first prime of the warp
+    // (parts past the last whole block start at it: the last part then
+    // holds just the partial block, whose start value is computed at `full`)
+    const uint32_t b_lo = min(full, j * part), b_hi = min(full, b_lo + part);
+    const bool last_part = j == nsplit - 1u;
     const uint64_t pi = base + lane;
     const bool valid = pi < np;
-    const uint64_t p = a.P[valid ? pi : base];
+    const uint64_t p = a.P[valid ? pi : (base < np ? base : 0)];
     q_p[wib][lane] = p;
     if (valid) {
       const uint64_t ps = a.Pinv ? a.Pinv[pi] : neg_inv64(p);
       const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = q_pinv<FORM>(ps, sh);
-      const uint64_t x = inv_pow2(nmin, p, ps);
+      const uint64_t x = inv_pow2(nmin + s * (uint32_t)U * b_lo, p, ps);
       const uint64_t K = a.proth ? p - x : x;
       uint32_t klo = lo32(K), khi = hi32(K);
       // twin: p - K is below the window bound `lim` iff K > p - lim, and its low
@@ -455,7 +475,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         tw_above = (lim != 0ull && p > lim) ? p - lim : 0ull;
         tw_low = lo32(p) & win_mask;
       }
-      for (uint32_t b = 0; b < full; ++b) {
+      for (uint32_t b = b_lo; b < b_hi; ++b) {
         uint32_t acc = 0xffffffffu;
         bool f = false;
 #pragma unroll
@@ -481,8 +501,8 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         }
       }
       // the last partial block (fewer than U steps) always goes to the queue,
-      // with its start value, which is at hand
-      if (full * (uint32_t)U < nsteps) {
+      // with its start value, which is at hand (in the last part)
+      if (last_part && full * (uint32_t)U < nsteps) {
         q_k[wib][lane] = mk64(klo, khi);
         const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
         if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | full;
@@ -523,15 +543,16 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
       }
     } else if (valid) {
       // queue overflow (not expected at the designed false-pass rates): each
-      // lane re-walks its own prime with the exact test at every step
+      // lane re-walks its own part of its prime with the exact test at every step
       const uint64_t p = q_p[wib][lane];
       const uint64_t ps = neg_inv64(p);
-      const uint64_t x = inv_pow2(nmin, p, ps);
+      const uint32_t t_lo = (uint32_t)U * b_lo, t_hi = last_part ? nsteps : (uint32_t)U * b_hi;
+      const uint64_t x = inv_pow2(nmin + s * t_lo, p, ps);
       const uint64_t K = a.proth ? p - x : x;
       uint32_t klo = lo32(K), khi = hi32(K);
       const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = q_pinv<FORM>(ps, sh);
 #pragma unroll 1
-      for (uint32_t t = 0; t < nsteps; ++t) {
+      for (uint32_t t = t_lo; t < t_hi; ++t) {
         const uint32_t idx = a.idx_base + (uint32_t)pi;
         record_exact(klo, khi, nmin + s * t, p, idx, a.kmin, a.kmax, a.nmax, a.hits, a.hit_count, a.hit_cap, s);
         if (TW) {

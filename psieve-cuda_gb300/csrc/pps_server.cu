@@ -57,6 +57,13 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
+// Estimated walk steps of the piece [lo, hi) of a job: primes ~ (hi - lo) /
+// ln lo, each walked over the job's whole n range.
+double piece_work(const pps_job_params& jp, uint64_t lo, uint64_t hi) {
+  const double nsteps = (double)((jp.nmax - jp.nmin + jp.step - 1) / jp.step);
+  return (double)(hi - lo) / log((double)std::max<uint64_t>(lo, 3)) * nsteps;
+}
+
 // Expected raw candidates of a job: sum over primes p in the range of
 // #k * #n / p, with sum 1/p over [a, b) ~ ln(ln b / ln a) (Mertens).
 uint64_t job_reservation(const pps_job_params& jp) {
@@ -126,28 +133,46 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
       failed.push_back(j);
     }
   }
-  // the wave: one piece per job first (oldest first), then fill oldest first
+  // The wave: one piece per job first (oldest first), each at most an equal
+  // share of the wave's work, then fill oldest first.  A wave holds at most
+  // wave_segments segments and about wave_work walk steps, so a job that
+  // arrives while it runs waits at most one such wave for its first piece.
   pieces.clear();
   const uint64_t cap = s->cfg.wave_segments;
+  const double work_cap = (double)s->cfg.wave_work;
   // a piece is at most one batch, and never more than the wave holds
   const uint64_t span = std::min<uint64_t>(batch_max_piece_span(), cap * 2ull * pps::SEG_BITS);
+  const uint64_t seg_span = 2ull * pps::SEG_BITS;  // p range of one segment
   uint64_t segs = 0;
+  double work = 0;
   std::vector<JobRec*> in_wave, finishing;
-  auto take = [&](JobRec* j) -> bool {
+  auto take = [&](JobRec* j, double share) -> bool {
     if (j->status || j->cursor >= j->jp.pmax) return false;
-    const uint64_t hi = std::min(j->jp.pmax, j->cursor + span);
+    uint64_t hi = std::min(j->jp.pmax, j->cursor + span);
+    // cut to the work left in the wave (or the share), whole segments, at least one
+    const double room = std::min(work_cap - work, share);
+    const double w = piece_work(j->jp, j->cursor, hi);
+    if (w > room) {
+      if (room <= 0 && !pieces.empty()) return false;
+      const double frac = std::max(room, 0.0) / w;
+      uint64_t width = (uint64_t)(frac * (double)(hi - j->cursor));
+      width = std::max<uint64_t>(seg_span, width / seg_span * seg_span);
+      hi = std::min(hi, j->cursor + width);
+    }
     const uint64_t ns = batch_piece_segments(j->cursor, hi);
     if (segs + ns > cap) return false;
     pieces.push_back(BatchPiece{j->cursor, hi, j->slot});
     segs += ns;
+    work += piece_work(j->jp, j->cursor, hi);
     j->cursor = hi;
     return true;
   };
+  const double first_share = act.empty() ? work_cap : work_cap / (double)act.size();
   for (JobRec* j : act)
-    if (take(j)) in_wave.push_back(j);
+    if (take(j, first_share)) in_wave.push_back(j);
   for (JobRec* j : act) {
     bool any = false;
-    while (take(j)) any = true;
+    while (work < work_cap && take(j, work_cap)) any = true;
     if (any && std::find(in_wave.begin(), in_wave.end(), j) == in_wave.end()) in_wave.push_back(j);
   }
   for (JobRec* j : act)
@@ -255,6 +280,7 @@ extern "C" int pps_server_create(int device, const pps_server_config* cfg, pps_s
     return set_err(PPS_ERR_INVALID_PARAM, "max_jobs above %u", batch_max_slots());
   if (!c.wave_segments || c.wave_segments > batch_wave_segments())
     c.wave_segments = (uint32_t)batch_wave_segments();
+  if (!c.wave_work) c.wave_work = 40000000000ull;
   pps_engine* e = nullptr;
   int rc = pps_engine_create(device, &e);
   if (rc) return rc;

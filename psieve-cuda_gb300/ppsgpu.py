@@ -66,7 +66,8 @@ class JobStats(ctypes.Structure):
                 ("steps", ctypes.c_uint64), ("batches", ctypes.c_uint32),
                 ("variant", ctypes.c_uint32), ("sieve_ms", ctypes.c_double),
                 ("walk_ms", ctypes.c_double), ("filter_ms", ctypes.c_double),
-                ("total_ms", ctypes.c_double)]
+                ("total_ms", ctypes.c_double), ("split", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -86,7 +87,7 @@ class BatchStats(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("factor_bytes", ctypes.c_uint64), ("max_jobs", ctypes.c_uint32),
-                ("wave_segments", ctypes.c_uint32)]
+                ("wave_segments", ctypes.c_uint32), ("wave_work", ctypes.c_uint64)]
 
 
 class JobResult(ctypes.Structure):
@@ -207,6 +208,7 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_engine_device_bytes": (ctypes.c_uint64, [ctypes.c_void_p]),
         "pps_engine_set_batch_span": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
         "pps_engine_set_variant": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+        "pps_engine_set_split": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
         "pps_engine_launches": (ctypes.c_uint64, [ctypes.c_void_p]),
         "pps_run_job": (ctypes.c_int, [ctypes.c_void_p, P(JobParams), ctypes.c_void_p,
                                        ctypes.c_size_t, szp, P(JobStats)]),
@@ -315,6 +317,10 @@ class Engine:
 
     def set_variant(self, v: int) -> None:
         _check(self.lib, self.lib.pps_engine_set_variant(self.h, v))
+
+    def set_split(self, t: int) -> None:
+        """Force the threads per prime of the queued walks (1, 2, 4, 8; 0: tuned)."""
+        _check(self.lib, self.lib.pps_engine_set_split(self.h, t))
 
     def set_input(self, inp: "InputFile | None") -> None:
         """Use an input sieve file as the output rule (None: the small-prime filter)."""
@@ -466,9 +472,9 @@ class Server:
     job's sorted factor list."""
 
     def __init__(self, device: int = 0, factor_bytes: int = 0, max_jobs: int = 0,
-                 wave_segments: int = 0, lib=None):
+                 wave_segments: int = 0, wave_work: int = 0, lib=None):
         self.lib = lib or load()
-        cfg = ServerConfig(factor_bytes, max_jobs, wave_segments)
+        cfg = ServerConfig(factor_bytes, max_jobs, wave_segments, int(wave_work))
         h = ctypes.c_void_p()
         _check(self.lib, self.lib.pps_server_create(device, ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h

@@ -54,3 +54,28 @@ def test_batch_repeat_and_degenerate(pps, engine, ora):
     # an empty batch is valid
     per, st = engine.run_batch([])
     assert per == [] and st.factors == 0
+
+
+@pytest.mark.parametrize("split", [2, 8])
+def test_batch_n_parts_match_oracle(pps, engine, ora, ref_cases, split):
+    """Each job's n range cut into `split` parts, each part its own work item
+    (forced here for every job, the short and the degenerate n ranges too):
+    every list is the reference's or the oracle's."""
+    names = sorted(k for k in ref_cases if k.startswith("rand"))[:16]
+    jobs = [pps.normalize(**args_to_spec(ref_cases[n]["args"])) for n in names]
+    extra = [
+        dict(pmin=42 * 10**12, pmax=42 * 10**12 + 10**6, kmin=1201, kmax=9999, nmin=2000000, nmax=2100003),
+        dict(pmin=(1 << 62) - 10**6, pmax=1 << 62, kmin=3, kmax=9999, nmin=1000, nmax=1002, sign=-1),
+        dict(pmin=10**12, pmax=10**12 + 10**7, kmin=3, kmax=9999, nmin=2000, nmax=3000, sign=pps.PPS_SIGN_TWIN),
+    ]
+    jobs += [pps.normalize(**s) for s in extra]
+    engine.set_split(split)
+    try:
+        per, _ = engine.run_batch(jobs)
+    finally:
+        engine.set_split(0)
+    for j, name in enumerate(names):
+        assert lines_of(pps.factors_to_tuples(per[j])) == sorted(set(ref_cases[name]["lines"])), name
+    for i, spec in enumerate(extra):
+        want, _, _ = ora.run(ora.normalize(**spec))
+        assert pps.factors_to_tuples(per[len(names) + i]) == ora.tuples(want), spec

@@ -217,3 +217,54 @@ def test_large_n_slice_per_line(pps, engine, ora):
     primes = ora.sieve_range(lo, lo + 2 * 10**8, jp.qmax)
     assert st.primes == len(primes)
     assert st.prime_sum == int(primes.sum(dtype=np.uint64))
+
+
+@pytest.mark.parametrize("split", [2, 8])
+def test_split_walks_match_oracle(pps, engine, ora, split):
+    """Threads per prime: each prime's n range cut into `split` parts walked by
+    their own threads (forced here), for each kind of queued walk, against the
+    oracle; the job shapes leave parts empty, or holding only the partial last
+    block, too."""
+    cases = [
+        # 32-bit steps, running-minimum window: 156 blocks + 3 steps
+        (15, dict(pmin=42 * 10**12, pmax=42 * 10**12 + 3 * 10**6, kmin=1201, kmax=9999, nmin=2000000,
+                  nmax=2040010)),
+        # 62-bit Riesel, single-bound pre-test: 156 blocks + 2 steps
+        (16, dict(pmin=(1 << 62) - (1 << 26), pmax=(1 << 62) - (1 << 26) + 2 * 10**6, kmin=3, kmax=9999,
+                  nmin=100000, nmax=140000, sign=-1)),
+        # 27-bit steps, window K < 2^s: 14 blocks, no partial one (8 parts: the last is empty)
+        (21, dict(pmin=10**12, pmax=10**12 + 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=5000)),
+        # a twin job (26-bit steps) through the prime-list path: 4 blocks + 7 steps
+        (24, dict(pmin=10**12, pmax=10**12 + 10**7, kmin=3, kmax=9999, nmin=2000, nmax=3000,
+                  sign=pps.PPS_SIGN_TWIN)),
+    ]
+    engine.set_split(split)
+    try:
+        for variant, spec in cases:
+            engine.set_variant(variant)
+            if spec.get("sign") == pps.PPS_SIGN_TWIN:
+                got, st = _gpu_lines_primes(pps, engine, ora, spec)
+            else:
+                got, st = _gpu_lines(pps, engine, spec)
+            want, cnt, _ = ora.run(ora.normalize(**spec))
+            assert (st.variant, st.split) == (variant, split)
+            assert got == lines_of(ora.tuples(want)), (split, spec)
+            assert st.primes == cnt
+    finally:
+        engine.set_split(0)
+        engine.set_variant(-1)
+
+
+def test_tuner_splits_small_prime_counts(pps, ref_cases):
+    """A job with far fewer primes than the GPU's resident threads (the
+    reference's 2e6-wide slice at 4.2e13: 63,903 primes, n over a million):
+    the tuner walks each prime with more than one thread, and the list is the
+    reference's."""
+    case = ref_cases["large_n_slice0"]
+    from helpers import args_to_spec
+
+    with pps.Engine(0) as eng:
+        fac, st = eng.run_job(pps.normalize(**args_to_spec(case["args"])))
+    assert st.split >= 2, st.split
+    assert lines_of(pps.factors_to_tuples(fac)) == sorted(set(case["lines"]))
+    assert st.primes == case["count"]
