@@ -297,10 +297,11 @@ def run_other_workloads(eng) -> dict:
         out[name] = {"primes": int(st.primes), "seconds": dt, "primes_per_s": st.primes / dt,
                      "n_steps_per_s": st.steps / dt, "factors": len(fac), "nstep": int(jp.nstep),
                      "walk_step": int(jp.step), "variant": int(st.variant), "split": int(st.split)}
-    # Few primes, long n: p in [4.2e13, 4.2e13 + 1e7) holds about 3.2e5 primes,
-    # about one wave of the GPU's resident threads.  The tuner's threads per
-    # prime against one thread per prime (forced), each timed after a warm-up.
-    jp = ppsgpu.normalize(**dict(LARGE_N, pmax=LARGE_N["pmin"] + 10**7))
+    # Few primes, long n: p in [4.2e13, 4.2e13 + 2e6) holds 63,903 primes, about
+    # a quarter of a wave of the walk's resident threads.  The chosen threads
+    # per prime against one thread per prime (forced), each timed after a
+    # warm-up.
+    jp = ppsgpu.normalize(**dict(LARGE_N, pmax=LARGE_N["pmin"] + 2 * 10**6))
     import numpy as np
 
     res, lists = {}, {}

@@ -127,6 +127,16 @@ const char *pps_version(void);
    is a retry loop, then exit (pps/appcu.cu:283-324). */
 int pps_debug_fail_allocs(int skip, int count);
 
+/* Test hook for the correctness fallbacks that only a wrong tuning choice
+   reaches: warp_queue caps the flagged blocks a warp of the queued walks
+   holds for its exact re-check (0..512; -1 = 512), so that warps whose queue
+   overflows re-walk their primes with the exact test at every step; and
+   first_candidates (0 = no cap) caps the raw-candidate buffer on the first
+   attempt of every call (and of every wave of the batched form), so that the
+   call finds it overflowed, grows the buffer and walks again.  Results are
+   unchanged; only speed is.  Applies to every engine from the next call. */
+int pps_debug_limits(int warp_queue, uint32_t first_candidates);
+
 /* Apply the reference's option rules (main.c:916-931, main.c:971-972,
    pps/app.c:657-712, pps/appcu.cu:158-204, pps/appcu.cu:236). */
 int pps_normalize(const pps_job_spec *in, pps_job_params *out);
@@ -147,13 +157,13 @@ int pps_engine_sm_count(const pps_engine *e);
 int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 
 /* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
-#define PPS_NUM_VARIANTS 26
+#define PPS_NUM_VARIANTS 30
 int pps_engine_set_variant(pps_engine *e, int variant);
 
 /* Force the threads per prime of the queued walks (1, 2, 4 or 8: each prime's
    n range is cut into that many parts walked side by side), or 0 for the
-   tuner's choice (timed per job size where a job has fewer primes than a few
-   waves of resident threads).  In the batched form and the serving loop the
+   choice per job (where a job's primes fill less than one wave of the walk's
+   resident threads, the smallest number of parts that fills it).  In the batched form and the serving loop the
    same number of n parts is used for every job (tuned: long n ranges are cut
    into parts of about the tuned work per chunk). */
 int pps_engine_set_split(pps_engine *e, int split);
@@ -247,6 +257,7 @@ typedef struct {
   uint64_t primes, prime_sum, raw_hits, factors, steps;
   uint32_t waves, chunk, unroll, pad;
   double total_ms, filter_ms;
+  double sieve_ms, walk_ms;  /* device time of the waves' sieve parts and walks */
 } pps_batch_stats;
 
 int pps_run_batch(pps_engine *e, const pps_job_params *jobs, size_t njobs, pps_factor *out,
@@ -277,7 +288,8 @@ typedef struct {
   uint64_t wave_work;      /* walk steps per wave, estimated from each piece's p range and n
                               range (primes ~ width / ln p); 0 = 4e10 (about 15 ms of the
                               GPU); a piece is at least one segment.  A job that arrives
-                              while a wave runs joins the next one, so this bounds its wait. */
+                              while a wave runs joins the next one, so this bounds its wait.
+                              With more than 4 jobs running it grows with them, up to 8x. */
 } pps_server_config;
 
 #define PPS_JOB_QUEUED  0  /* submitted, waiting for admission */

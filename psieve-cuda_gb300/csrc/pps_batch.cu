@@ -98,10 +98,16 @@ struct BatchState {
   const uint32_t* qm_q = nullptr;  // sieving-prime table the constants belong to
   uint32_t qm_n = 0;
   uint64_t prime_cap = 0;
-  cudaGraphExec_t graph = nullptr;
+  // the wave's launch sequence as two captured graphs: the sieve part (clear,
+  // scatter, segment sieve, scans, expansion, chunking) and the walk, so that
+  // events between the two launches time each part
+  cudaGraphExec_t graph = nullptr, graph_walk = nullptr;
+  cudaEvent_t ev_wave[3] = {nullptr, nullptr, nullptr};
+  double sieve_ms = 0, walk_ms = 0;  // device time of the waves so far, per part
   int graph_unroll = 0;
   const uint32_t* graph_q = nullptr;  // sieving-prime table the graph was captured with
   uint32_t graph_nq = 0;
+  uint32_t graph_hcap = 0, graph_qcap = 0;  // candidate and warp-queue capacities it was captured with
   cudaEvent_t copied = nullptr;
   int tuned_work = 0, tuned_unroll = 0;  // walk steps per chunk (x32 lanes), inner unroll
   std::vector<BJob> hjobs;               // host mirror of the device job slots
@@ -109,10 +115,19 @@ struct BatchState {
   DevBuf<unsigned long long> bak_primes, bak_sum;  // slot counters before a wave
 };
 
+void drop_graphs(BatchState* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->graph_walk) cudaGraphExecDestroy(b->graph_walk);
+  b->graph = nullptr;
+  b->graph_walk = nullptr;
+}
+
 void batch_state_free(pps_engine* e) {
   BatchState* b = e->batch;
   if (!b) return;
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  drop_graphs(b);
+  for (auto& v : b->ev_wave)
+    if (v) cudaEventDestroy(v);
   if (b->copied) cudaEventDestroy(b->copied);
   if (b->h_tables) cudaFreeHost(b->h_tables);
   b->tables.release();
@@ -523,7 +538,7 @@ __device__ __forceinline__ uint32_t b_pinv(uint64_t ps, uint32_t s) {
 template <int FORM, int U, int TEST, bool TW>
 __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint32_t part, uint64_t p, uint64_t ps,
                                         bool valid, uint32_t* qe, uint32_t* qc, uint64_t* qp, uint64_t* qk,
-                                        pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
+                                        uint32_t qcap, pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t s = FORM == 0 ? 32u : J.step;
   const uint32_t nsteps = J.nsteps, full = nsteps / (uint32_t)U;
@@ -578,19 +593,19 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint32_t pa
       f |= TEST == 2 ? acc <= bound_hi : acc == 0u;
       if (f) {
         const uint32_t pos = atomicAdd(qc, 1u);
-        if (pos < BQ_CAP) qe[pos] = (lane << 27) | b;
+        if (pos < qcap) qe[pos] = (lane << 27) | b;
       }
     }
     if (last_part && full * (uint32_t)U < nsteps) {
       // the partial last block: its start value is at hand, keep it
       qk[lane] = mk64(klo, khi);
       const uint32_t pos = atomicAdd(qc, 1u);
-      if (pos < BQ_CAP) qe[pos] = (lane << 27) | full;
+      if (pos < qcap) qe[pos] = (lane << 27) | full;
     }
   }
   __syncwarp();
   const uint32_t cnt = *qc;
-  if (cnt <= BQ_CAP) {
+  if (cnt <= qcap) {
     for (uint32_t e = lane; e < cnt; e += 32u) {
       const uint32_t ent = qe[e];
       const uint32_t owner = ent >> 27, blk = ent & ((1u << 27) - 1u);
@@ -649,7 +664,7 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
                                                          const uint32_t* seg_count, const uint32_t* seg_off,
                                                          const uint32_t* chunk_off, const uint32_t* chunk_seg,
                                                          const uint64_t* P, const uint64_t* Pinv, uint64_t* tot,
-                                                         uint64_t chunk_limit, pps_hit* hits,
+                                                         uint64_t chunk_limit, uint32_t qcap, pps_hit* hits,
                                                          uint32_t* hit_count, uint32_t hit_cap) {
   __shared__ uint32_t q_ent[BW_THREADS / 32][BQ_CAP];
   __shared__ uint64_t q_p[BW_THREADS / 32][32];
@@ -682,7 +697,7 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
       const uint64_t p = P[pi], ps = Pinv[pi];
 #define PPS_BROUND(FORM_, TEST_, TW_)                                                                    \
   b_round<FORM_, U, TEST_, TW_>(J, job, part, p, ps, valid, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib], \
-                                hits, hit_count, hit_cap)
+                                qcap, hits, hit_count, hit_cap)
 #define PPS_BROUND_F(FORM_)                                                                             \
   do {                                                                                                  \
     if (wsh) {                                                                                          \
@@ -780,6 +795,11 @@ int ensure_state(pps_engine* e) {
       b->copied = nullptr;
       return set_err(PPS_ERR_CUDA, "event");
     }
+    for (auto& v : b->ev_wave)
+      if (!v && cudaEventCreate(&v) != cudaSuccess) {
+        v = nullptr;
+        return set_err(PPS_ERR_CUDA, "event");
+      }
     // job slots at their maximum size once: the captured graph holds these pointers
     if ((rc = b->jobs.ensure(MAX_JOBS)) || (rc = b->job_primes.ensure(MAX_JOBS)) ||
         (rc = b->job_sum.ensure(MAX_JOBS)) || (rc = b->bak_primes.ensure(MAX_JOBS)) ||
@@ -796,9 +816,9 @@ int ensure_state(pps_engine* e) {
 
 constexpr uint64_t WAVE_KERNELS = 11;  // kernels in one wave's launch sequence
 
-// The fixed per-wave launch sequence (everything reads counts from the tables).
-int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, uint64_t chunk_limit,
-                pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
+// The fixed per-wave launch sequence (everything reads counts from the
+// tables): the sieve part, then the walk.
+int launch_wave_sieve(pps_engine* e, const uint32_t* dq, uint32_t nq_all) {
   BatchState* b = e->batch;
   cudaStream_t st = e->st;
   k_bclear<<<e->num_sms * 8, 256, 0, st>>>(b->tables.p, b->bitmap.p);
@@ -816,16 +836,31 @@ int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, 
   k_bscan<<<1, 1024, 0, st>>>(b->chunk_count.p, b->chunk_off.p, WAVE_SEGS, b->tot.p + 2);
   k_bchunkmap<<<WAVE_SEGS, 256, 0, st>>>(b->tables.p, b->chunk_count.p, b->chunk_off.p, b->chunk_seg.p,
                                          b->chunk_seg.n);
+  CU(cudaGetLastError());
+  e->launches += WAVE_KERNELS - 1;
+  return PPS_OK;
+}
+
+int launch_wave_walk(pps_engine* e, int unroll, uint64_t chunk_limit, pps_hit* hits, uint32_t* hit_count,
+                     uint32_t hit_cap) {
+  BatchState* b = e->batch;
+  cudaStream_t st = e->st;
   int per_sm = 0;
   auto fn = unroll == 16 ? k_bwalk<16> : k_bwalk<8>;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
   const int grid = (per_sm > 0 ? per_sm : 1) * e->num_sms;
   fn<<<grid, BW_THREADS, 0, st>>>(b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p,
-                                  b->chunk_seg.p, b->P.p, b->Pinv.p, b->tot.p, chunk_limit, hits, hit_count,
-                                  hit_cap);
+                                  b->chunk_seg.p, b->P.p, b->Pinv.p, b->tot.p, chunk_limit,
+                                  std::min(debug_queue_cap(), BQ_CAP), hits, hit_count, hit_cap);
   CU(cudaGetLastError());
-  e->launches += WAVE_KERNELS;
+  e->launches += 1;
   return PPS_OK;
+}
+
+int launch_wave(pps_engine* e, const uint32_t* dq, uint32_t nq_all, int unroll, uint64_t chunk_limit,
+                pps_hit* hits, uint32_t* hit_count, uint32_t hit_cap) {
+  int rc = launch_wave_sieve(e, dq, nq_all);
+  return rc ? rc : launch_wave_walk(e, unroll, chunk_limit, hits, hit_count, hit_cap);
 }
 
 int floor_lg2(uint64_t x) { return 63 - __builtin_clzll(x | 1ull); }
@@ -1035,8 +1070,7 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
   if (b->qm_q != dq || b->qm_n != nq_all) {
     // a new sieving-prime table: its Barrett constants (the graph, which holds
     // the old qm pointer, is recaptured too)
-    if (b->graph) cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
+    drop_graphs(b);
     b->qm_q = nullptr;
     b->qm_n = 0;
     if ((rc = b->qm.ensure(std::max<uint32_t>(nq_all, 1)))) return rc;
@@ -1116,7 +1150,8 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
         fn<<<std::max(per_sm, 1) * e->num_sms, BW_THREADS, 0, st>>>(
             b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p, b->chunk_seg.p, b->P.p,
-            b->Pinv.p, b->tot.p, lim, b->out.p, b->counters.p + 2, (uint32_t)b->out.n);
+            b->Pinv.p, b->tot.p, lim, std::min(debug_queue_cap(), BQ_CAP), b->out.p, b->counters.p + 2,
+            (uint32_t)b->out.n);
         CU(cudaGetLastError());
         e->launches++;
         CU(cudaEventRecord(e->ev[1], st));
@@ -1145,36 +1180,59 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
   // the wave itself: a captured graph of the fixed sequence, replayed
   CU(cudaMemsetAsync(b->counters.p, 0, 2 * sizeof(uint32_t), st));
   uint32_t raw = 0;
+  // the first attempt's candidate capacity (less under pps_debug_limits)
+  uint32_t hcap = (uint32_t)std::min<size_t>(b->hits.n, 0xffffffffu);
+  if (debug_first_hit_cap() && debug_first_hit_cap() < hcap) hcap = debug_first_hit_cap();
   for (;;) {
-    if (!b->graph || b->graph_unroll != b->tuned_unroll || b->graph_q != dq || b->graph_nq != nq_all) {
-      if (b->graph) cudaGraphExecDestroy(b->graph);
-      b->graph = nullptr;
-      cudaGraph_t g;
-      CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      const uint64_t launches0 = e->launches;
-      rc = launch_wave(e, dq, nq_all, b->tuned_unroll, 0, b->hits.p, b->counters.p, (uint32_t)b->hits.n);
-      cudaError_t ce = cudaStreamEndCapture(st, &g);
-      e->launches = launches0;
-      if (rc) return rc;
-      if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&b->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    const uint32_t qcap = std::min(debug_queue_cap(), BQ_CAP);
+    if (!b->graph || !b->graph_walk || b->graph_unroll != b->tuned_unroll || b->graph_q != dq ||
+        b->graph_nq != nq_all || b->graph_hcap != hcap || b->graph_qcap != qcap) {
+      drop_graphs(b);
+      for (int part = 0; part < 2; ++part) {
+        cudaGraph_t g;
+        CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const uint64_t launches0 = e->launches;
+        rc = part == 0 ? launch_wave_sieve(e, dq, nq_all)
+                       : launch_wave_walk(e, b->tuned_unroll, 0, b->hits.p, b->counters.p, hcap);
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        e->launches = launches0;
+        if (rc) return rc;
+        if (ce != cudaSuccess) return set_err(PPS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(part == 0 ? &b->graph : &b->graph_walk, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+          drop_graphs(b);
+          return set_err(PPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+        }
+      }
       b->graph_unroll = b->tuned_unroll;
       b->graph_q = dq;
       b->graph_nq = nq_all;
+      b->graph_hcap = hcap;
+      b->graph_qcap = qcap;
     }
+    CU(cudaEventRecord(b->ev_wave[0], st));
     CU(cudaGraphLaunch(b->graph, st));
+    CU(cudaEventRecord(b->ev_wave[1], st));
+    CU(cudaGraphLaunch(b->graph_walk, st));
+    CU(cudaEventRecord(b->ev_wave[2], st));
     e->launches += WAVE_KERNELS;
     CU(cudaMemcpyAsync(e->h_pinned, b->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
+    {
+      float ms0 = 0, ms1 = 0;
+      CU(cudaEventElapsedTime(&ms0, b->ev_wave[0], b->ev_wave[1]));
+      CU(cudaEventElapsedTime(&ms1, b->ev_wave[1], b->ev_wave[2]));
+      b->sieve_ms += ms0;
+      b->walk_ms += ms1;
+    }
     raw = ((uint32_t*)e->h_pinned)[0];
-    if (raw <= b->hits.n) break;
+    if (raw <= hcap) break;
     // more candidates than the buffer: grow it (a new graph), put the slot
     // counters back and walk the wave again
-    if (b->graph) cudaGraphExecDestroy(b->graph);  // it holds the old hits pointer
-    b->graph = nullptr;
-    if ((rc = b->hits.ensure((size_t)raw * 2))) return rc;
+    drop_graphs(b);  // the walk graph holds the old hits pointer
+    if (raw > b->hits.n && (rc = b->hits.ensure((size_t)raw * 2))) return rc;
+    hcap = (uint32_t)std::min<size_t>(b->hits.n, 0xffffffffu);
     if ((rc = restore())) return rc;
     CU(cudaMemsetAsync(b->counters.p, 0, 2 * sizeof(uint32_t), st));
   }
@@ -1225,6 +1283,7 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
   if ((rc = batch_prepare(e))) return rc;
   BatchState* b = e->batch;
   if (bst) memset(bst, 0, sizeof *bst);
+  b->sieve_ms = b->walk_ms = 0;
   CU(cudaEventRecord(e->ev[6], e->st));
 
   // jobs j in slots j; pieces of at most one batch, most expensive jobs first
@@ -1297,6 +1356,8 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
     bst->total_ms = ms;
     bst->filter_ms = fms;
+    bst->sieve_ms = b->sieve_ms;
+    bst->walk_ms = b->walk_ms;
   }
   if (out && nf > cap) return set_err(PPS_ERR_OVERFLOW, "%zu factors, buffer holds %zu", nf, cap);
   return PPS_OK;

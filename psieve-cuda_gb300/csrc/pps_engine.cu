@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -66,6 +67,18 @@ extern "C" int pps_debug_fail_allocs(int skip, int count) {
   g_fail_done = 0;
   return (int)done;
 }
+static std::atomic<uint32_t> g_dbg_qcap{(uint32_t)WALK_QUEUE_CAP}, g_dbg_hitcap{0};
+
+uint32_t debug_queue_cap() { return g_dbg_qcap.load(std::memory_order_relaxed); }
+uint32_t debug_first_hit_cap() { return g_dbg_hitcap.load(std::memory_order_relaxed); }
+
+extern "C" int pps_debug_limits(int warp_queue, uint32_t first_candidates) {
+  if (warp_queue > WALK_QUEUE_CAP) return set_err(PPS_ERR_INVALID_PARAM, "warp queue above %d", WALK_QUEUE_CAP);
+  g_dbg_qcap = warp_queue < 0 ? (uint32_t)WALK_QUEUE_CAP : (uint32_t)warp_queue;
+  g_dbg_hitcap = first_candidates;
+  return PPS_OK;
+}
+
 extern "C" const char* pps_version(void) { return "ppsgpu-0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------ normalize
@@ -426,6 +439,7 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
   a->nsteps = (jp->nmax - jp->nmin + jp->step - 1) / jp->step;
   if (jp->nmax == jp->nmin) a->nsteps = 0;
   a->proth = jp->sign == 1 ? 1u : 0u;
+  a->qcap = debug_queue_cap();
   // window pre-test parameters
   const int kb = lg2u64(jp->kmax) + 1;         // kmax < 2^kb
   const int lp = lg2u64(jp->pmin);
@@ -447,29 +461,32 @@ static void fill_walk_args(const pps_job_params* jp, WalkArgs* a) {
 }
 
 static int variant_ok(const pps_job_params* jp, int v) {
-  // variants 22-25 walk both sides of a twin job; every other variant one side
+  const VariantTraits& t = walk_variant_traits(v);
+  // the twin variants walk both sides of a twin job; every other variant one side
   const bool twin = jp->sign == PPS_SIGN_TWIN;
-  if (twin != (v >= 22)) return 0;
-  if ((v == 7 || v == 8) && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
-  if (((v >= 10 && v <= 18) || v == 22 || v == 23) && jp->step != 32) return 0;  // 32-bit steps
-  if (v >= 18) {
+  if (twin != t.twin) return 0;
+  if (t.lowbit && jp->kmax >= (1ull << 32)) return 0;  // low-bit test needs kmax < 2^32
+  if (t.s32 && jp->step != 32) return 0;
+  if (t.shifted || t.smallp || t.min_window) {
     WalkArgs a;
     fill_walk_args(jp, &a);
-    const bool shifted = (v >= 19 && v <= 21) || v >= 24, smallp = v == 18 || v == 20 || v == 23 || v == 25;
-    // (variants 19 and 21, the window K < 2^s on the step's shifted words, need only walk form 1)
-    if (shifted && !a.shift_ok) return 0;    // shifted chain: s < 32, p <= 2^(32+s)
-    if (smallp && a.sh_t >= 32) return 0;    // small-p window
+    if (t.shifted && !a.shift_ok) return 0;   // shifted chain: s < 32, p <= 2^(32+s)
+    if (t.smallp && a.sh_t >= 32) return 0;   // small-p window
+    if (t.min_window && a.win_hi != 0) return 0;  // running-minimum window: u == 0
   }
-  if (v == 10 || v == 13 || v == 15) {                            // running-minimum window: u == 0
-    WalkArgs a;
-    fill_walk_args(jp, &a);
-    if (a.win_hi != 0) return 0;
-  }
-  if (v == 12 || v == 14 || v == 16) {  // single bound: kmax < 2^32, false-pass rate below 2^-12
+  if (t.bound) {  // single bound: kmax < 2^32, false-pass rate below 2^-12
     if (jp->kmax >= (1ull << 32)) return 0;
     if (jp->pmin / jp->kmax < (1ull << 43)) return 0;
   }
   return 1;
+}
+
+// The raw-candidate capacity of this attempt: the buffer's size, or less under
+// pps_debug_limits.
+static uint32_t hit_cap_now(const pps_engine* e) {
+  size_t c = std::min<size_t>(e->hits.n, 0xffffffffu);
+  if (e->hit_cap_limit && e->hit_cap_limit < c) c = e->hit_cap_limit;
+  return (uint32_t)c;
 }
 
 static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64_t* dP, const uint64_t* dPinv,
@@ -478,8 +495,9 @@ static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64
   WalkArgs a;
   fill_walk_args(jp, &a);
   if (nsteps_cap && a.nsteps > nsteps_cap) a.nsteps = nsteps_cap;
-  // threads per prime: queued walks only (variants 10 and up)
-  a.nsplit = v >= 10 && split > 1 ? split : 1;
+  // threads per prime: queued walks only
+  const VariantTraits& vt = walk_variant_traits(v);
+  a.nsplit = vt.queued && split > 1 ? split : 1;
   a.P = dP;
   a.Pinv = dPinv;
   a.d_np = d_np;
@@ -487,19 +505,21 @@ static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64
   a.idx_base = idx_base;
   a.hits = e->hits.p;
   a.hit_count = e->counters.p;
-  a.hit_cap = (uint32_t)std::min<size_t>(e->hits.n, 0xffffffffu);
+  a.hit_cap = hit_cap_now(e);
   const int threads = 256;
   int maxb = walk_max_blocks(v, threads, jp->step, e->num_sms);
   if (maxb <= 0) return set_err(PPS_ERR_CUDA, "walk variant %d unavailable", v);
-  const uint64_t nvirt = v >= 10 ? ((np_max + 31) & ~31ull) * a.nsplit : np_max;
+  // queued walks: a warp covers 32 x per_thread primes of one n part
+  const uint64_t wp = 32ull * (uint64_t)vt.per_thread;
+  const uint64_t nvirt = vt.queued ? (np_max + wp - 1) / wp * 32ull * a.nsplit : np_max;
   uint64_t need = (nvirt + threads - 1) / threads;
-  // The queued walks (variants 10 and up) get one thread per prime: the block
+  // The queued walks get one thread per prime (or per primes_per_thread): the block
   // scheduler then hands new primes to whichever SM has finished its blocks, so
   // every SM keeps its full complement of warps to the end (with a grid of one
   // resident wave that loops over the primes, the warps the scheduler favours
   // finish their share early and the SMs run the rest at reduced occupancy).
   // The older walks keep one resident wave (their ILP forms stride over it).
-  const uint64_t cap = v >= 10 ? 0x7fffffffull : (uint64_t)maxb;
+  const uint64_t cap = vt.queued ? 0x7fffffffull : (uint64_t)maxb;
   int blocks = (int)std::min<uint64_t>(cap, need ? need : 1);
   CU(launch_walk(v, a, blocks, threads, e->st));
   e->launches++;
@@ -529,23 +549,23 @@ static bool tune_log() {
 static double pretest_pass_rate(const pps_job_params* jp, int v) {
   WalkArgs a;
   fill_walk_args(jp, &a);
+  const VariantTraits& t = walk_variant_traits(v);
   const double p = (double)jp->pmin, kmax = (double)jp->kmax;
   const int kb = lg2u64(jp->kmax) + 1;
-  const bool smallp = v == 18 || v == 20 || v == 23 || v == 25;
   double r;
-  if (v == 12 || v == 14 || v == 16) {
+  if (t.bound) {
     r = kmax * 2147483648.0 / p;
-  } else if (v == 7 || v == 8) {
+  } else if (t.lowbit) {
     r = kmax * 4294967296.0 / p;
-  } else if (smallp) {
+  } else if (t.smallp) {
     r = ldexp(1.0, (int)a.sh_t) / p + ldexp(1.0, -((int)a.sh_t + 1 - kb));
-  } else if (v == 19 || v == 21) {
+  } else if (t.stepwin) {
     r = ldexp(1.0, (int)jp->step) / p + ldexp(1.0, kb - 1 - (int)jp->step);
   } else {
     const int u = a.win_hi == 0xffffffffu ? 32 : __builtin_popcount(a.win_hi);
     r = ldexp(1.0, 32 + u) / p + (a.win_mask == 0xffffffffu ? ldexp(1.0, -32) : 1.0 / ((double)a.win_mask + 1.0));
   }
-  if (v >= 22) r *= 2.0;
+  if (t.twin) r *= 2.0;
   return std::min(r, 1.0);
 }
 
@@ -553,14 +573,17 @@ static double pretest_pass_rate(const pps_job_params* jp, int v) {
 // exact for it whose pre-test passes at most 1 step in 512 and, for the queued
 // walks, whose expected queue load over the whole n range fits in half the
 // warp queue; every exact variant where none does.
-static uint32_t variant_set(const pps_job_params* jp) {
+static uint64_t variant_set(const pps_job_params* jp) {
   const double nsteps_full = jp->nmax > jp->nmin ? (double)((jp->nmax - jp->nmin + jp->step - 1) / jp->step) : 0.0;
-  uint32_t exact = 0, cls = 0;
+  uint64_t exact = 0, cls = 0;
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v)
     if (variant_ok(jp, v)) {
-      exact |= 1u << v;
+      const VariantTraits& t = walk_variant_traits(v);
+      exact |= 1ull << v;
       const double r = pretest_pass_rate(jp, v);
-      if (r <= 1.0 / 512.0 && (v < 10 || 32.0 * nsteps_full * r <= WALK_QUEUE_CAP / 2)) cls |= 1u << v;
+      // a warp's queue holds the flagged blocks of its 32 x per_thread primes
+      const double lanes = 32.0 * t.per_thread;
+      if (r <= 1.0 / 512.0 && (!t.queued || lanes * nsteps_full * r <= WALK_QUEUE_CAP / 2)) cls |= 1ull << v;
     }
   return cls ? cls : exact;
 }
@@ -578,7 +601,7 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   // overflows on the full range (each lane then re-walks its prime exactly);
   // and without the rate bound a choice timed on one job could be reused for a
   // job of the same kind at much smaller p, where its window passes most steps.
-  const uint32_t cls = variant_set(jp);
+  const uint64_t cls = variant_set(jp);
   // jobs are told apart by that set (step size, side, window kind, bound test,
   // pass rates): a choice is reused only within the same set
   // a forced variant is honoured only where it is exact for this job
@@ -601,12 +624,14 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   int best = -1;
   float best_ms = 1e30f;  // per prime of the sample
   for (int v = 0; v < PPS_NUM_VARIANTS; ++v) {
-    if (!(cls & (1u << v))) continue;
-    // each variant is timed on whole waves of its own grid (one thread per
-    // prime), so that a variant with fewer resident blocks per SM is not timed
+    if (!(cls & (1ull << v))) continue;
+    // each variant is timed on one whole wave of its own grid (one thread per
+    // prime, or per two for the two-prime walks) where the job has that many
+    // primes, so that a variant with fewer resident blocks per SM is not timed
     // with a partly idle last wave
-    const uint64_t wave = (uint64_t)walk_max_blocks(v, 256, jp->step, e->num_sms) * 256;
-    const uint64_t sv = std::min<uint64_t>(sample, wave ? wave : sample);
+    const uint64_t wave = (uint64_t)walk_max_blocks(v, 256, jp->step, e->num_sms) * 256 *
+                          (uint64_t)walk_variant_traits(v).per_thread;
+    const uint64_t sv = std::min<uint64_t>(np, wave ? wave : sample);
     CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
     int rc = run_walk(e, jp, v, dP, dPinv, nullptr, sv, 0, cap_steps);  // warm-up
     if (rc) return rc;
@@ -641,53 +666,25 @@ static int ceil_lg(uint64_t x) {
 }
 
 // Threads per prime for the queued walk v on np primes (1 where the walk is not
-// a queued one).  Where the job's primes fill fewer than four waves of resident
-// threads, the last wave leaves SMs idle; cutting each prime's n range into T
-// parts fills them, at the cost of one more start value (an exponentiation) per
-// part.  T in {1, 2, 4, 8} (parts of at least 32 blocks) is timed on the job's
-// own primes with the same total steps for every T, and the choice is kept per
-// (variant set, variant, log2 primes, log2 steps).
-static int choose_split(pps_engine* e, const pps_job_params* jp, uint32_t cls, int v, const uint64_t* dP,
-                        const uint64_t* dPinv, uint64_t np) {
-  if (v < 10 || np == 0) return 1;
+// a queued one).  Where the job's primes fill less than one wave of the
+// walk's resident threads R, most SMs would idle for the whole walk; cutting
+// each prime's n range into T parts (T np >= R, T <= 8, parts of at least 32
+// blocks) fills them, at the cost of one more start value (an
+// exponentiation) per part.  From one wave up, T = 1: the partial last wave
+// then costs little (a lightly loaded SM runs its warps faster), and timing T
+// per job cost more than it saved on a 512-job mix of distinct jobs (measured
+// on the GB300: 3.2e5 primes, 1.37 waves, ran 5% faster with T = 2).
+static int choose_split(pps_engine* e, const pps_job_params* jp, int v, uint64_t np) {
+  const VariantTraits& vt = walk_variant_traits(v);
+  if (!vt.queued || np == 0) return 1;
   if (e->forced_split > 0) return e->forced_split;
   WalkArgs a;
   fill_walk_args(jp, &a);
-  const uint32_t U = (v == 13 || v == 14) ? 16u : 8u;
-  const uint32_t blocks = a.nsteps / U;
-  const uint64_t resident = (uint64_t)walk_max_blocks(v, 256, jp->step, e->num_sms) * 256;
-  if (resident == 0 || np >= 4 * resident || blocks < 64) return 1;
-  const int lg_np = ceil_lg(np), lg_steps = ceil_lg(a.nsteps);
-  for (const auto& t : e->tuned_split)
-    if (t.mask == cls && t.variant == v && t.lg_np == lg_np && t.lg_steps == lg_steps) return (int)t.split;
-  // the same total steps for every T (at most 16384 per prime), so that
-  // only the wave fill and the per-part start values differ
-  const uint32_t cap = std::min<uint32_t>(a.nsteps, 16384);
-  uint32_t best = 1;
-  float best_ms = 1e30f;
-  for (uint32_t T = 1; T <= 8; T *= 2) {
-    if (T > 1 && cap / U < 32 * T) break;
-    int rc;
-    CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
-    if ((rc = run_walk(e, jp, v, dP, dPinv, nullptr, np, 0, cap, T))) return rc;  // warm-up
-    CU(cudaEventRecord(e->ev[6], e->st));
-    for (int r = 0; r < 2; ++r)
-      if ((rc = run_walk(e, jp, v, dP, dPinv, nullptr, np, 0, cap, T))) return rc;
-    CU(cudaEventRecord(e->ev[7], e->st));
-    CU(cudaEventSynchronize(e->ev[7]));
-    float ms = 0;
-    CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
-    if (tune_log())
-      fprintf(stderr, "pps tune: variant %d, %llu primes, %u steps: split %u %.3f ms\n", v,
-              (unsigned long long)np, cap, T, ms);
-    if (ms < best_ms * 0.97f) {  // a larger T must win clearly
-      best_ms = ms;
-      best = T;
-    }
-  }
-  CU(cudaMemsetAsync(e->counters.p, 0, sizeof(uint32_t), e->st));
-  e->tuned_split.push_back({cls, v, lg_np, lg_steps, best});
-  return (int)best;
+  const uint64_t blocks = a.nsteps / (uint32_t)vt.unroll;
+  const uint64_t resident = (uint64_t)walk_max_blocks(v, 256, jp->step, e->num_sms) * 256 * vt.per_thread;
+  int t = 1;
+  while (t < 8 && np * (uint64_t)t < resident && blocks / (2ull * t) >= 32) t *= 2;
+  return t;
 }
 
 static int ensure_hit_buffers(pps_engine* e, size_t hit_cap, size_t fac_cap) {
@@ -740,7 +737,7 @@ static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, 
   CU(cudaStreamSynchronize(e->st));
   const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
   *raw_hits_out = raw;
-  if (raw > e->hits.n) {
+  if (raw > hit_cap_now(e)) {
     *overflow = true;
     return PPS_OK;
   }
@@ -748,7 +745,7 @@ static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, 
   FilterArgs f;
   f.hits = e->hits.p;
   f.d_nhits = e->counters.p;
-  f.hit_cap = (uint32_t)std::min<size_t>(e->hits.n, 0xffffffffu);
+  f.hit_cap = hit_cap_now(e);
   f.kstep = jp->kstep;
   f.koffset = jp->koffset;
   f.nmin = jp->nmin;
@@ -826,7 +823,7 @@ static int run_job_once(pps_engine* e, const pps_job_params* jp, pps_factor* out
       if (variant < 0) return variant;
       if (st) st->variant = (uint32_t)variant;
     }
-    const int split = choose_split(e, jp, variant_set(jp), variant, e->P.p, e->Pinv.p, np);
+    const int split = choose_split(e, jp, variant, np);
     if (split < 0) return split;
     if (st) st->split = std::max<uint32_t>(st->split, (uint32_t)split);
     CU(cudaEventRecord(e->ev[2], e->st));
@@ -883,6 +880,7 @@ extern "C" int pps_run_job(pps_engine* e, const pps_job_params* jp, pps_factor* 
   for (int attempt = 0; attempt < 4; ++attempt) {
     int rc = ensure_hit_buffers(e, std::max(hit_cap, e->hits.n), std::max(fac_cap, e->factors.n));
     if (rc) return rc;
+    e->hit_cap_limit = attempt == 0 ? debug_first_hit_cap() : 0;
     if (st) memset(st, 0, sizeof *st);
     bool overflow = false;
     cudaEventRecord(e->ev[6], e->st);
@@ -896,8 +894,11 @@ extern "C" int pps_run_job(pps_engine* e, const pps_job_params* jp, pps_factor* 
       if (st) st->total_ms = ms;
       return PPS_OK;
     }
-    hit_cap = e->hits.n * 4;
-    fac_cap = e->factors.n * 4;
+    // grow the buffers, unless the overflow was only the first attempt's
+    // debug cap (the retry lifts it)
+    const size_t grow = attempt == 0 && debug_first_hit_cap() ? 1 : 4;
+    hit_cap = e->hits.n * grow;
+    fac_cap = e->factors.n * grow;
   }
   return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "hit buffer overflow persisted");
 }
@@ -908,7 +909,7 @@ static int walk_device_list(pps_engine* e, const pps_job_params* jp, const uint6
   int variant = autotune(e, jp, dP, nullptr, np);
   if (variant < 0) return variant;
   if (st) st->variant = (uint32_t)variant;
-  const int split = choose_split(e, jp, variant_set(jp), variant, dP, nullptr, np);
+  const int split = choose_split(e, jp, variant, np);
   if (split < 0) return split;
   if (st) st->split = (uint32_t)split;
   CU(cudaEventRecord(e->ev[2], e->st));
@@ -936,6 +937,7 @@ extern "C" int pps_check_primes_device(pps_engine* e, const pps_job_params* jp, 
   for (int attempt = 0; attempt < 4; ++attempt) {
     int rc = ensure_hit_buffers(e, std::max(hit_cap, e->hits.n), std::max(fac_cap, e->factors.n));
     if (rc) return rc;
+    e->hit_cap_limit = attempt == 0 ? debug_first_hit_cap() : 0;
     if (st) memset(st, 0, sizeof *st);
     CU(cudaMemsetAsync(e->counters.p, 0, 2 * sizeof(uint32_t), e->st));
     if (np && (rc = walk_device_list(e, jp, d_P, np, st))) return rc;
@@ -944,8 +946,11 @@ extern "C" int pps_check_primes_device(pps_engine* e, const pps_job_params* jp, 
     rc = finish_job(e, jp, out, cap, nout, st, &raw, &overflow);
     if (st) st->raw_hits = raw;
     if (rc || !overflow) return rc;
-    hit_cap = e->hits.n * 4;
-    fac_cap = e->factors.n * 4;
+    // grow the buffers, unless the overflow was only the first attempt's
+    // debug cap (the retry lifts it)
+    const size_t grow = attempt == 0 && debug_first_hit_cap() ? 1 : 4;
+    hit_cap = e->hits.n * grow;
+    fac_cap = e->factors.n * grow;
   }
   return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "hit buffer overflow persisted");
 }
@@ -977,13 +982,14 @@ extern "C" int pps_check_primes_raw(pps_engine* e, const pps_job_params* jp, con
   size_t hit_cap = std::max<size_t>(1u << 20, e->hits.n);
   for (int attempt = 0; attempt < 4; ++attempt) {
     if ((rc = ensure_hit_buffers(e, hit_cap, std::max<size_t>(1u << 18, e->factors.n)))) return rc;
+    e->hit_cap_limit = attempt == 0 ? debug_first_hit_cap() : 0;
     CU(cudaMemsetAsync(e->counters.p, 0, 2 * sizeof(uint32_t), e->st));
     if (np && (rc = walk_device_list(e, jp, e->P.p, np, nullptr))) return rc;
     CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
     CU(cudaStreamSynchronize(e->st));
     const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
-    if (raw > e->hits.n) {
-      hit_cap = (size_t)raw * 2;
+    if (raw > hit_cap_now(e)) {
+      hit_cap = std::max<size_t>(hit_cap, raw > e->hits.n ? (size_t)raw * 2 : e->hits.n);
       continue;
     }
     std::vector<pps_hit> tmp(raw);

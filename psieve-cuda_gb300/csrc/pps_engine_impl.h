@@ -23,6 +23,10 @@ int set_err(int code, const char* fmt, ...);
 // Host-side fault injection (pps_debug_fail_allocs): true when this device
 // allocation is to fail as if device memory were exhausted.
 bool alloc_fault_injected();
+// pps_debug_limits: the warp-queue cap of the queued walks (512 unless set) and
+// the raw-candidate cap of each call's first attempt (0: none).
+uint32_t debug_queue_cap();
+uint32_t debug_first_hit_cap();
 
 // Device buffer that only grows (contents are not preserved on growth).  A
 // failed growth leaves it empty (p null, n 0): whatever cached a pointer into
@@ -70,7 +74,7 @@ struct pps_engine {
   // tuned walk variant per set of exact variants (bit v: variant v is exact),
   // with the work (primes x steps) of the sample it was timed on
   struct Tuned {
-    uint32_t mask;
+    uint64_t mask;
     int variant;
     uint64_t work;
   };
@@ -78,8 +82,9 @@ struct pps_engine {
   // threads per prime of the queued walks: forced (0: tuned), and the tuned
   // choice per (variant set, variant, log2 primes, log2 steps)
   int forced_split = 0;
+  uint32_t hit_cap_limit = 0;  // the raw-candidate cap of this attempt (0: the buffer's size)
   struct TunedSplit {
-    uint32_t mask;
+    uint64_t mask;
     int variant;
     int lg_np, lg_steps;
     uint32_t split;

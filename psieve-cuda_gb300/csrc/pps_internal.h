@@ -60,6 +60,7 @@ struct WalkArgs {
   uint32_t nsplit;          // queued walks: threads per prime (1, 2, 4, 8): thread j of a
                             // prime walks blocks [j L, (j+1) L) of its n range,
                             // L = ceil(blocks / nsplit); 0 counts as 1
+  uint32_t qcap;            // queued walks: warp-queue entries used (<= WALK_QUEUE_CAP)
   uint32_t idx_base;        // added to the prime index in hit records
   pps_hit* hits;
   uint32_t* hit_count;      // may exceed hit_cap: overflow is detected by host
@@ -72,6 +73,28 @@ struct WalkArgs {
 constexpr int WALK_QUEUE_CAP = 512;
 
 const char* walk_variant_name(int v);
+// What a walk variant is: the queued walks (k_walk32q, k_walk32q2) hold no
+// exact-check code in their hot loop and take threads per prime; the others
+// (k_walk) branch or replay per block.  Pre-test kinds: window (hi word below
+// 2^u or the low bits zero), min (the window as a running minimum, u == 0),
+// bound (hi word <= kmax/2: 32-bit steps, p > kmax 2^43), lowbit (kmax <
+// 2^32), smallp (K < 2^t or the low bits zero, p far below 2^(64-bits(kmax))),
+// stepwin (K < 2^s read off the step, s < 32).
+struct VariantTraits {
+  const char* name;
+  bool queued;
+  bool twin;       // both sides of a twin job from one walk
+  bool s32;        // 32-bit steps only
+  bool shifted;    // s < 32 through the carry-free step on K 2^(32-s) (p <= 2^(32+s))
+  bool smallp;
+  bool min_window; // needs u == 0
+  bool bound;
+  bool lowbit;
+  bool stepwin;
+  int unroll;      // steps per block
+  int per_thread;  // primes per thread (queued walks: a warp covers 32 x this)
+};
+const VariantTraits& walk_variant_traits(int v);
 // Pre-test constants of a normalised job, and whether variant v is exact for it
 // (defined in pps_engine.cu).
 void walk_args_for_job(const pps_job_params* jp, WalkArgs* a);

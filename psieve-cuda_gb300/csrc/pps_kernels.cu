@@ -446,6 +446,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
   const uint64_t nvirt = npad * nsplit;
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const uint64_t wstride = (uint64_t)gridDim.x * blockDim.x;
+  const uint32_t qcap = min(a.qcap, (uint32_t)WQ_CAP);  // entries used (a test hook lowers it)
   if (lane == 0) q_cnt[wib] = 0;
   __syncwarp();
   for (uint64_t vbase = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); vbase < nvirt;
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
         if (TEST == 0 || TEST == 3) f |= acc == 0u;
         if (f) {
           const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
-          if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | b;
+          if (pos < qcap) q_ent[wib][pos] = (lane << 27) | b;
         }
       }
       // the last partial block (fewer than U steps) always goes to the queue,
@@ -505,12 +506,12 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
       if (last_part && full * (uint32_t)U < nsteps) {
         q_k[wib][lane] = mk64(klo, khi);
         const uint32_t pos = atomicAdd(&q_cnt[wib], 1u);
-        if (pos < WQ_CAP) q_ent[wib][pos] = (lane << 27) | full;
+        if (pos < qcap) q_ent[wib][pos] = (lane << 27) | full;
       }
     }
     __syncwarp();
     const uint32_t cnt = q_cnt[wib];
-    if (cnt <= (uint32_t)WQ_CAP) {
+    if (cnt <= qcap) {
       // re-check the queued blocks exactly, one block per lane
       for (uint32_t e = lane; e < cnt; e += 32u) {
         const uint32_t ent = q_ent[wib][e];
@@ -569,23 +570,175 @@ __global__ void __launch_bounds__(256, MINB) k_walk32q(WalkArgs a) {
   }
 }
 
-struct VariantDesc {
-  const char* name;
-};
-static const VariantDesc kVariants[PPS_NUM_VARIANTS] = {
-    {"form0-window-u4-step"}, {"chain-window-u4-step"}, {"chain-window-u8-block"},
-    {"form2-window-u8-block"}, {"form0-window-u8-block"}, {"chain-window-u8-block-ilp2"},
-    {"form2-window-u8-block-ilp2"}, {"chain-lowbit-u8-block"}, {"form0-lowbit-u8-block"},
-    {"chain-window-u16-block"}, {"queue-min-u8"}, {"queue-window-u8"}, {"queue-bound-u8"},
-    {"queue-min-u16"}, {"queue-bound-u16"}, {"queue-min-u8-r40"}, {"queue-bound-u8-r40"},
-    {"queue-window-u8-r40"}, {"queue-smallp-u8"}, {"queue-shift-hiwin-u8"}, {"queue-shift-smallp-u8"},
-    {"queue-shift-hiwin-u8-r40"}, {"twin-window-u8"}, {"twin-smallp-u8"}, {"twin-shift-window-u8"},
-    {"twin-shift-smallp-u8"},
+// ---- queued walk, two primes per thread.  The same walk as k_walk32q for
+// 32-bit steps (window as a running minimum, TEST 0, or the single bound,
+// TEST 2), with lane l of a warp walking primes base + l and base + 32 + l
+// side by side, so that each thread holds two independent step chains (their
+// multiplies interleave).  A warp covers 64 primes of one n part; queue
+// entries carry the prime's slot (0..63) in their top 6 bits.
+template <int TEST, int U, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_walk32q2(WalkArgs a) {
+  __shared__ uint32_t q_ent[WQ_WARPS][WQ_CAP];
+  __shared__ uint64_t q_p[WQ_WARPS][64];
+  __shared__ uint64_t q_k[WQ_WARPS][64];
+  __shared__ uint32_t q_cnt[WQ_WARPS];
+  const uint64_t np = a.d_np ? *a.d_np : a.np;
+  const uint32_t win_mask = a.win_mask, bound_hi = a.bound_hi;
+  const uint32_t nsteps = a.nsteps, nmin = a.nmin;
+  const uint32_t full = nsteps / (uint32_t)U;
+  const uint32_t nsplit = a.nsplit > 1u ? a.nsplit : 1u;
+  const uint32_t part = (full + nsplit - 1u) / nsplit;
+  const uint64_t npad = (np + 63ull) & ~63ull;  // primes, rounded to whole warps of 64
+  const uint64_t nwarps = npad / 64 * nsplit;
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint64_t wstride = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t qcap = min(a.qcap, (uint32_t)WQ_CAP);
+  if (lane == 0) q_cnt[wib] = 0;
+  __syncwarp();
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += wstride) {
+    const uint64_t wpp = npad / 64;  // warps per part
+    const uint32_t j = (uint32_t)(w / wpp);
+    const uint64_t base = (w - (uint64_t)j * wpp) * 64;
+    const uint32_t b_lo = min(full, j * part), b_hi = min(full, b_lo + part);
+    const bool last_part = j == nsplit - 1u;
+    const uint64_t pi0 = base + lane, pi1 = base + 32 + lane;
+    const bool v0 = pi0 < np, v1 = pi1 < np;
+    const uint64_t p0 = a.P[v0 ? pi0 : base], p1 = a.P[v1 ? pi1 : base];
+    q_p[wib][lane] = p0;
+    q_p[wib][32 + lane] = p1;
+    if (v0) {
+      const uint64_t ps0 = a.Pinv ? a.Pinv[pi0] : neg_inv64(p0);
+      const uint64_t ps1 = v1 ? (a.Pinv ? a.Pinv[pi1] : neg_inv64(p1)) : ps0;
+      const uint32_t plon0 = neg_lo(p0), phi10 = neg_hi(p0), pinv0 = lo32(ps0);
+      const uint32_t plon1 = neg_lo(p1), phi11 = neg_hi(p1), pinv1 = lo32(ps1);
+      const uint32_t n0 = nmin + 32u * (uint32_t)U * b_lo;
+      const uint64_t x0 = inv_pow2(n0, p0, ps0), x1 = inv_pow2(n0, p1, ps1);
+      const uint64_t K0 = a.proth ? p0 - x0 : x0, K1 = a.proth ? p1 - x1 : x1;
+      uint32_t klo0 = lo32(K0), khi0 = hi32(K0), klo1 = lo32(K1), khi1 = hi32(K1);
+      for (uint32_t b = b_lo; b < b_hi; ++b) {
+        uint32_t acc0 = 0xffffffffu, acc1 = 0xffffffffu;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (TEST == 0) {
+            acc0 = min(acc0, min(khi0, klo0 & win_mask));
+            acc1 = min(acc1, min(khi1, klo1 & win_mask));
+          } else {
+            acc0 = min(acc0, khi0);
+            acc1 = min(acc1, khi1);
+          }
+          step_neg32(klo0, khi0, plon0, phi10, pinv0);
+          step_neg32(klo1, khi1, plon1, phi11, pinv1);
+        }
+        const bool f0 = TEST == 2 ? acc0 <= bound_hi : acc0 == 0u;
+        const bool f1 = v1 && (TEST == 2 ? acc1 <= bound_hi : acc1 == 0u);
+        if (f0 | f1) {
+          const uint32_t pos = atomicAdd(&q_cnt[wib], (uint32_t)f0 + (uint32_t)f1);
+          if (f0 && pos < qcap) q_ent[wib][pos] = (lane << 26) | b;
+          if (f1 && pos + (uint32_t)f0 < qcap) q_ent[wib][pos + (uint32_t)f0] = ((32u + lane) << 26) | b;
+        }
+      }
+      if (last_part && full * (uint32_t)U < nsteps) {
+        q_k[wib][lane] = mk64(klo0, khi0);
+        q_k[wib][32 + lane] = mk64(klo1, khi1);
+        const uint32_t pos = atomicAdd(&q_cnt[wib], 1u + (uint32_t)v1);
+        if (pos < qcap) q_ent[wib][pos] = (lane << 26) | full;
+        if (v1 && pos + 1u < qcap) q_ent[wib][pos + 1u] = ((32u + lane) << 26) | full;
+      }
+    }
+    __syncwarp();
+    const uint32_t cnt = q_cnt[wib];
+    if (cnt <= qcap) {
+      for (uint32_t e = lane; e < cnt; e += 32u) {
+        const uint32_t ent = q_ent[wib][e];
+        const uint32_t owner = ent >> 26, blk = ent & ((1u << 26) - 1u);
+        const uint64_t op = q_p[wib][owner];
+        const uint64_t ops = neg_inv64(op);
+        const uint32_t t0 = (uint32_t)U * blk;
+        const uint32_t nblk = min((uint32_t)U, nsteps - t0);
+        const uint32_t n0 = nmin + 32u * t0;
+        uint64_t K;
+        if (blk == full) {
+          K = q_k[wib][owner];
+        } else {
+          const uint64_t x = inv_pow2(n0, op, ops);
+          K = a.proth ? op - x : x;
+        }
+        uint32_t klo = lo32(K), khi = hi32(K);
+        const uint32_t oplon = neg_lo(op), ophi1 = neg_hi(op), opinv = lo32(ops);
+        const uint32_t idx = a.idx_base + (uint32_t)(base + owner);
+#pragma unroll 1
+        for (uint32_t u = 0; u < nblk; ++u) {
+          record_exact(klo, khi, n0 + 32u * u, op, idx, a.kmin, a.kmax, a.nmax, a.hits, a.hit_count, a.hit_cap);
+          step_neg32(klo, khi, oplon, ophi1, opinv);
+        }
+      }
+    } else {
+      // queue overflow: each lane re-walks its part of its two primes with the
+      // exact test at every step
+      for (int which = 0; which < 2; ++which) {
+        const uint64_t pi = which ? pi1 : pi0;
+        if (pi >= np) continue;
+        const uint64_t p = q_p[wib][which * 32 + lane];
+        const uint64_t ps = neg_inv64(p);
+        const uint32_t t_lo = (uint32_t)U * b_lo, t_hi = last_part ? nsteps : (uint32_t)U * b_hi;
+        const uint64_t x = inv_pow2(nmin + 32u * t_lo, p, ps);
+        const uint64_t K = a.proth ? p - x : x;
+        uint32_t klo = lo32(K), khi = hi32(K);
+        const uint32_t plon = neg_lo(p), phi1 = neg_hi(p), pinv = lo32(ps);
+        const uint32_t idx = a.idx_base + (uint32_t)pi;
+#pragma unroll 1
+        for (uint32_t t = t_lo; t < t_hi; ++t) {
+          record_exact(klo, khi, nmin + 32u * t, p, idx, a.kmin, a.kmax, a.nmax, a.hits, a.hit_count, a.hit_cap);
+          step_neg32(klo, khi, plon, phi1, pinv);
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) q_cnt[wib] = 0;
+    __syncwarp();
+  }
+}
+
+// name, queued, twin, s32, shifted, smallp, min_window, bound, lowbit, stepwin, unroll, per_thread
+static const VariantTraits kVariants[PPS_NUM_VARIANTS] = {
+    {"form0-window-u4-step", false, false, false, false, false, false, false, false, false, 4, 1},
+    {"chain-window-u4-step", false, false, false, false, false, false, false, false, false, 4, 1},
+    {"chain-window-u8-block", false, false, false, false, false, false, false, false, false, 8, 1},
+    {"form2-window-u8-block", false, false, false, false, false, false, false, false, false, 8, 1},
+    {"form0-window-u8-block", false, false, false, false, false, false, false, false, false, 8, 1},
+    {"chain-window-u8-block-ilp2", false, false, false, false, false, false, false, false, false, 8, 1},
+    {"form2-window-u8-block-ilp2", false, false, false, false, false, false, false, false, false, 8, 1},
+    {"chain-lowbit-u8-block", false, false, false, false, false, false, false, true, false, 8, 1},
+    {"form0-lowbit-u8-block", false, false, false, false, false, false, false, true, false, 8, 1},
+    {"chain-window-u16-block", false, false, false, false, false, false, false, false, false, 16, 1},
+    {"queue-min-u8", true, false, true, false, false, true, false, false, false, 8, 1},
+    {"queue-window-u8", true, false, true, false, false, false, false, false, false, 8, 1},
+    {"queue-bound-u8", true, false, true, false, false, false, true, false, false, 8, 1},
+    {"queue-min-u16", true, false, true, false, false, true, false, false, false, 16, 1},
+    {"queue-bound-u16", true, false, true, false, false, false, true, false, false, 16, 1},
+    {"queue-min-u8-r40", true, false, true, false, false, true, false, false, false, 8, 1},
+    {"queue-bound-u8-r40", true, false, true, false, false, false, true, false, false, 8, 1},
+    {"queue-window-u8-r40", true, false, true, false, false, false, false, false, false, 8, 1},
+    {"queue-smallp-u8", true, false, true, false, true, false, false, false, false, 8, 1},
+    {"queue-shift-hiwin-u8", true, false, false, true, false, false, false, false, true, 8, 1},
+    {"queue-shift-smallp-u8", true, false, false, true, true, false, false, false, false, 8, 1},
+    {"queue-shift-hiwin-u8-r40", true, false, false, true, false, false, false, false, true, 8, 1},
+    {"twin-window-u8", true, true, true, false, false, false, false, false, false, 8, 1},
+    {"twin-smallp-u8", true, true, true, false, true, false, false, false, false, 8, 1},
+    {"twin-shift-window-u8", true, true, false, true, false, false, false, false, false, 8, 1},
+    {"twin-shift-smallp-u8", true, true, false, true, true, false, false, false, false, 8, 1},
+    {"queue2-min-u8", true, false, true, false, false, true, false, false, false, 8, 2},
+    {"queue2-bound-u8", true, false, true, false, false, false, true, false, false, 8, 2},
+    {"queue-min-u16-r40", true, false, true, false, false, true, false, false, false, 16, 1},
+    {"queue-bound-u16-r40", true, false, true, false, false, false, true, false, false, 16, 1},
 };
 
-const char* walk_variant_name(int v) {
-  return (v >= 0 && v < PPS_NUM_VARIANTS) ? kVariants[v].name : "?";
+const VariantTraits& walk_variant_traits(int v) {
+  static const VariantTraits none = {"?", false, false, false, false, false, false, false, false, false, 8, 1};
+  return (v >= 0 && v < PPS_NUM_VARIANTS) ? kVariants[v] : none;
 }
+
+const char* walk_variant_name(int v) { return walk_variant_traits(v).name; }
 
 typedef void (*walk_fn)(WalkArgs);
 
@@ -618,6 +771,10 @@ static walk_fn pick(int v) {
     case 23: return S32 ? k_walk32q<1, 8, 8, 0, true, true> : nullptr;
     case 24: return S32 ? nullptr : k_walk32q<1, 8, 8, 1, false, true>;
     case 25: return S32 ? nullptr : k_walk32q<1, 8, 8, 1, true, true>;
+    case 26: return S32 ? k_walk32q2<0, 8, 5> : nullptr;
+    case 27: return S32 ? k_walk32q2<2, 8, 5> : nullptr;
+    case 28: return S32 ? k_walk32q<0, 16, 6> : nullptr;
+    case 29: return S32 ? k_walk32q<2, 16, 6> : nullptr;
   }
   return nullptr;
 }

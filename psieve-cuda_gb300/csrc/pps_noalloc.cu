@@ -152,7 +152,7 @@ extern "C" int pps_check_primes_noalloc(const pps_job_params* jp, const uint64_t
     // the queued walks get one thread per prime (the block scheduler keeps every
     // SM full to the end); the block walks one resident wave that strides
     const uint64_t need = (np + 255) / 256;
-    const uint64_t cap = v >= 10 ? 0x7fffffffull : (uint64_t)maxb;
+    const uint64_t cap = walk_variant_traits(v).queued ? 0x7fffffffull : (uint64_t)maxb;
     const int blocks = (int)(need < cap ? need : cap);
     e = launch_walk(v, a, blocks, 256, st);
     if (e != cudaSuccess) return fail(PPS_ERR_CUDA, "walk launch: %s", cudaGetErrorString(e));

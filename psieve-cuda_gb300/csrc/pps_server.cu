@@ -137,9 +137,13 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
   // share of the wave's work, then fill oldest first.  A wave holds at most
   // wave_segments segments and about wave_work walk steps, so a job that
   // arrives while it runs waits at most one such wave for its first piece.
+  // Under load (more than 4 jobs running) the work per wave grows with the
+  // running jobs, up to 8 times, so that the per-wave cost (host turns, the
+  // last chunks' tail) stays small next to the walk.
   pieces.clear();
   const uint64_t cap = s->cfg.wave_segments;
-  const double work_cap = (double)s->cfg.wave_work;
+  const double load = std::min(8.0, std::max(1.0, (double)act.size() / 4.0));
+  const double work_cap = (double)s->cfg.wave_work * load;
   // a piece is at most one batch, and never more than the wave holds
   const uint64_t span = std::min<uint64_t>(batch_max_piece_span(), cap * 2ull * pps::SEG_BITS);
   const uint64_t seg_span = 2ull * pps::SEG_BITS;  // p range of one segment

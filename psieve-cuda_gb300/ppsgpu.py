@@ -31,7 +31,8 @@ PPS_ERR_TIMEOUT = -303
 PPS_ERR_BUSY = -304
 PPS_ERR_NOT_FOUND = -305
 PPS_ERR_CANCELLED = -306
-PPS_NUM_VARIANTS = 26
+PPS_NUM_VARIANTS = 30
+TWIN_VARIANTS = (22, 23, 24, 25)  # the walks of both sides of a twin job
 PPS_SIGN_TWIN = 2  # both sides from one walk (the reference's twin build)
 PPS_NOALLOC_MAX_PRIMES = 1 << 24  # per call of pps_check_primes_noalloc
 PPS_NOALLOC_MAX_CANDIDATES = 1 << 16
@@ -79,7 +80,8 @@ class BatchStats(ctypes.Structure):
                 ("steps", ctypes.c_uint64), ("waves", ctypes.c_uint32),
                 ("chunk", ctypes.c_uint32), ("unroll", ctypes.c_uint32),
                 ("pad", ctypes.c_uint32), ("total_ms", ctypes.c_double),
-                ("filter_ms", ctypes.c_double)]
+                ("filter_ms", ctypes.c_double), ("sieve_ms", ctypes.c_double),
+                ("walk_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
@@ -202,6 +204,7 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_last_error": (ctypes.c_char_p, []),
         "pps_version": (ctypes.c_char_p, []),
         "pps_debug_fail_allocs": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+        "pps_debug_limits": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32]),
         "pps_normalize": (ctypes.c_int, [P(JobSpec), P(JobParams)]),
         "pps_engine_create": (ctypes.c_int, [ctypes.c_int, P(ctypes.c_void_p)]),
         "pps_engine_destroy": (None, [ctypes.c_void_p]),

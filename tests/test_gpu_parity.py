@@ -78,7 +78,7 @@ def test_every_walk_variant_matches_oracle(pps, engine, ora, variant):
         dict(pmin=(1 << 62) - (1 << 26), pmax=(1 << 62) - (1 << 26) + 2 * 10**6, kmin=3, kmax=9999,
              nmin=100000, nmax=140000, sign=-1),
     ]
-    if variant >= 22:  # the twin kernels walk twin jobs (both sides)
+    if variant in pps.TWIN_VARIANTS:  # the twin kernels walk twin jobs (both sides)
         specs = [dict(s, sign=pps.PPS_SIGN_TWIN) for s in specs]
     engine.set_variant(variant)
     ran = 0
