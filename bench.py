@@ -254,15 +254,40 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
         eng.run_job(jp)
     eng.run_batch(jobs[: min(len(jobs), 64)])
     t0 = time.perf_counter()
-    plain, plain_primes = [], 0
+    plain, plain_primes, pst = [], 0, []
     for jp in jobs:
         fac, st = eng.run_job(jp)
         plain.append(fac)
         plain_primes += st.primes
+        pst.append(st)
     t_plain = time.perf_counter() - t0
     t0 = time.perf_counter()
     per, bst = eng.run_batch(jobs)
     t_batch = time.perf_counter() - t0
+    # where the time goes: device time per phase, the rest is host turns
+    # (launches, syncs, copies, tuning) and, for the plain form, the tuner's runs
+    sieve = sum(x.sieve_ms for x in pst)
+    walk = sum(x.walk_ms for x in pst)
+    filt = sum(x.filter_ms for x in pst)
+    breakdown = {
+        "plain": {"sieve_ms": sieve, "walk_ms": walk, "filter_ms": filt,
+                  "other_ms": t_plain * 1e3 - sieve - walk - filt,
+                  "walk_steps_per_s": sum(x.steps for x in pst) / (walk * 1e-3)},
+        "batched": {"sieve_ms": bst.sieve_ms, "walk_ms": bst.walk_ms, "filter_ms": bst.filter_ms,
+                    "other_ms": t_batch * 1e3 - bst.sieve_ms - bst.walk_ms - bst.filter_ms,
+                    "walk_steps_per_s": bst.steps / (bst.walk_ms * 1e-3) if bst.walk_ms else None}}
+    # the plain form's walk rate per kind of job (32-bit steps or shorter; n range)
+    classes = {}
+    for jp, x in zip(jobs, pst):
+        key = f"{'s32' if jp.step == 32 else 's<32'}_{'n<1e4' if jp.nmax - jp.nmin < 10**4 else 'n>=1e4'}"
+        c = classes.setdefault(key, {"jobs": 0, "steps": 0, "walk_ms": 0.0, "other_ms": 0.0})
+        c["jobs"] += 1
+        c["steps"] += x.steps
+        c["walk_ms"] += x.walk_ms
+        c["other_ms"] += x.total_ms - x.walk_ms
+    for c in classes.values():
+        c["walk_steps_per_s"] = c["steps"] / (c["walk_ms"] * 1e-3) if c["walk_ms"] else None
+    breakdown["plain_by_kind"] = classes
     identical = len(per) == len(plain) and all(np.array_equal(a, b) for a, b in zip(per, plain))
     job_primes, job_sums = eng.batch_job_primes(len(jobs))
     checked = {"jobs": jobs, "lists": per, "job_primes": job_primes, "job_sums": job_sums}
@@ -273,7 +298,7 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
             "plain_primes_per_s": plain_primes / t_plain, "batched_primes_per_s": bst.primes / t_batch,
             "speedup": t_plain / t_batch, "identical_results": bool(identical),
             "waves": int(bst.waves), "chunk": int(bst.chunk), "unroll": int(bst.unroll),
-            "batched_n_steps_per_s": bst.steps / t_batch}
+            "batched_n_steps_per_s": bst.steps / t_batch, "breakdown": breakdown}
 
 
 def run_other_workloads(eng) -> dict:
@@ -322,10 +347,12 @@ def run_other_workloads(eng) -> dict:
     return out
 
 
-def _serve_rate(srv, pool, nxt: int, rng, rate: float, window: float, max_jobs: int, served: list) -> tuple:
+def _serve_rate(srv, pool, nxt: int, rng, rate: float, window: float, max_jobs: int, served: list,
+                capacity: float | None = None) -> tuple:
     """Poisson arrivals at `rate` jobs/s for `window` seconds or `max_jobs` jobs,
     whichever ends first, then every job waited for.  Latency = submission to
-    result ready (the serving loop's own clock)."""
+    result ready (the serving loop's own clock).  With `capacity` (walk steps/s
+    of the whole GPU), each job's wait = latency - its own walk at that rate."""
     import numpy as np
 
     ids, jps = [], []
@@ -360,7 +387,9 @@ def _serve_rate(srv, pool, nxt: int, rng, rate: float, window: float, max_jobs: 
     # (the largest jobs' latency is mostly their own walk)
     med = rank(work, 0.5) if work else 0
     small = [l for l, w in zip(lat, work) if w <= med]
-    return nxt, {"rate_jobs_per_s": rate, "jobs": len(ids), "offered_s": submit_s, "seconds": elapsed,
+    waits = [l - 1e3 * w / capacity for l, w in zip(lat, work)] if capacity else []
+    extra = {"wait_p50_ms": rank(waits, 0.50), "wait_p99_ms": rank(waits, 0.99)} if capacity else {}
+    return nxt, {**extra, "rate_jobs_per_s": rate, "jobs": len(ids), "offered_s": submit_s, "seconds": elapsed,
                  "achieved_jobs_per_s": len(ids) / elapsed, "primes_per_s": primes / elapsed,
                  "n_steps_per_s": sum(work) / elapsed, "factors": factors,
                  "p50_ms": rank(lat, 0.50), "p99_ms": rank(lat, 0.99), "max_ms": max(lat) if lat else None,
@@ -368,14 +397,17 @@ def _serve_rate(srv, pool, nxt: int, rng, rate: float, window: float, max_jobs: 
 
 
 def run_serving(rates=(10.0, 30.0, 100.0, 300.0, 1000.0), window: float = 4.0, max_jobs: int = 400,
-                long_rate: float = 30.0, long_window: float = 60.0, seed: int = 3) -> tuple:
+                long_rate: float = 30.0, long_window: float = 60.0, seed: int = 3,
+                capacity: float | None = None) -> tuple:
     """The serving loop (pps_server_*): Poisson arrivals of jobs from the
     mixed-job distribution at each rate for `window` seconds or `max_jobs`
     jobs (so the rates above capacity, where a queue builds, still end), then
     one `long_window`-second window at `long_rate` (below capacity).  Reports
     per rate the aggregate primes/s and walk steps/s (first submission to last
     result) and the p50/p99 latency of all jobs and of the smaller half by
-    walk work.  Returns ((job, factors) of every served job, summary)."""
+    walk work, and (given `capacity`, the batched form's walk steps/s) of each
+    job's wait: its latency less its own walk at that rate, the delay the
+    serving loop adds.  Returns ((job, factors) of every served job, summary)."""
     import numpy as np
 
     import ppsgpu
@@ -389,11 +421,11 @@ def run_serving(rates=(10.0, 30.0, 100.0, 300.0, 1000.0), window: float = 4.0, m
             srv.wait(srv.submit(jp))
         nxt = 8
         for rate in rates:
-            nxt, r = _serve_rate(srv, pool, nxt, rng, rate, window, max_jobs, served)
+            nxt, r = _serve_rate(srv, pool, nxt, rng, rate, window, max_jobs, served, capacity)
             per_rate.append(r)
         long = None
         if long_window > 0:
-            nxt, long = _serve_rate(srv, pool, nxt, rng, long_rate, long_window, 1 << 30, served)
+            nxt, long = _serve_rate(srv, pool, nxt, rng, long_rate, long_window, 1 << 30, served, capacity)
         st = srv.stats()
     return served, {"workload": f"Poisson arrivals, {window:g} s or {max_jobs} jobs per rate, then "
                                 f"{long_window:g} s at {long_rate:g} jobs/s; jobs of the mixed-job distribution "
@@ -713,8 +745,9 @@ def run_gpu(args) -> None:
                           "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
     cpu = None if args.no_cpu else baseline_sample(args.ref_seconds)
     mixed_checked, batched = (None, None) if args.no_batched else run_mixed(eng, args.mixed_jobs)
-    served, serving = (None, None) if args.no_serving else run_serving(window=args.serve_window,
-                                                                       long_window=args.serve_long)
+    served, serving = (None, None) if args.no_serving else run_serving(
+        window=args.serve_window, long_window=args.serve_long,
+        capacity=batched["batched_n_steps_per_s"] if batched else None)
     others = None if args.no_batched else run_other_workloads(eng)
     verify = None if args.no_verify else run_checks(eng, args, slice_params, seq, timed_lists,
                                                     e2e_lists if e2e else None, mixed_checked, served)
@@ -763,6 +796,8 @@ def run_profile_batched(args) -> None:
     import ppsgpu
 
     eng = ppsgpu.Engine(0)
+    if args.wave_segments:
+        eng.set_wave_segments(args.wave_segments)  # smaller waves: less device memory (captures)
     jobs, _ = ppsgpu.mixed_jobs(seed=1, count=args.mixed_jobs)
     eng.run_batch(jobs[:64])
     t0 = time.perf_counter()
@@ -796,6 +831,8 @@ def main() -> None:
     ap.add_argument("--walk-variant", type=int, default=-1,
                     help="fix the walk kernel of the large-n Proth jobs (default: tuned)")
     ap.add_argument("--profile-batched", action="store_true")
+    ap.add_argument("--wave-segments", type=int, default=0,
+                    help="--profile-batched: segments per wave (0: the maximum, 16384)")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

@@ -157,7 +157,7 @@ int pps_engine_sm_count(const pps_engine *e);
 int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 
 /* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
-#define PPS_NUM_VARIANTS 30
+#define PPS_NUM_VARIANTS 33
 int pps_engine_set_variant(pps_engine *e, int variant);
 
 /* Force the threads per prime of the queued walks (1, 2, 4 or 8: each prime's
@@ -262,6 +262,13 @@ typedef struct {
 
 int pps_run_batch(pps_engine *e, const pps_job_params *jobs, size_t njobs, pps_factor *out,
                   size_t cap, size_t *nout, size_t *job_offsets, pps_batch_stats *st);
+
+/* Segments (2^18 odd candidates each) one wave of the batched form holds, at
+   most and by default 16384 (2^32 odd candidates: about 7.5 GB of wave
+   buffers).  Fewer hold proportionally less device memory (a profiler
+   capture, a shared GPU).  Only before the engine's first batched call
+   (PPS_ERR_BUSY after it). */
+int pps_engine_set_wave_segments(pps_engine *e, uint32_t segments);
 
 /* Per-job prime count and wrapping prime sum of the last pps_run_batch. */
 int pps_batch_job_primes(pps_engine *e, size_t njobs, uint64_t *primes, uint64_t *sums);

@@ -109,6 +109,7 @@ struct BatchState {
   uint32_t graph_nq = 0;
   uint32_t graph_hcap = 0, graph_qcap = 0;  // candidate and warp-queue capacities it was captured with
   cudaEvent_t copied = nullptr;
+  uint32_t wave_segs = WAVE_SEGS;  // segments one wave holds (pps_engine_set_wave_segments)
   int tuned_work = 0, tuned_unroll = 0;  // walk steps per chunk (x32 lanes), inner unroll
   std::vector<BJob> hjobs;               // host mirror of the device job slots
   std::vector<uint64_t> slot_pmax;       // each slot's pmax (sieving-prime bound)
@@ -777,17 +778,18 @@ int ensure_state(pps_engine* e) {
       b->h_tables = nullptr;
       return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "pinned table staging");
     }
-    if ((rc = b->bitmap.ensure((size_t)WAVE_SEGS * SEG_WORDS))) return rc;
+    b->wave_segs = e->wave_segs_req ? e->wave_segs_req : WAVE_SEGS;
+    if ((rc = b->bitmap.ensure((size_t)b->wave_segs * SEG_WORDS))) return rc;
     if ((rc = b->seg_count.ensure(WAVE_SEGS)) || (rc = b->seg_off.ensure(WAVE_SEGS)) ||
         (rc = b->chunk_count.ensure(WAVE_SEGS)) || (rc = b->chunk_off.ensure(WAVE_SEGS)) ||
         (rc = b->large_items.ensure(WAVE_BATCHES)) || (rc = b->large_off.ensure(WAVE_BATCHES)))
       return rc;
     // p > 2^32: odd primes are fewer than 1/10 of the odd candidates
-    b->prime_cap = (uint64_t)WAVE_SEGS * SEG_BITS / 10 + 4096;
+    b->prime_cap = (uint64_t)b->wave_segs * SEG_BITS / 10 + 4096;
     if ((rc = b->P.ensure(b->prime_cap)) || (rc = b->Pinv.ensure(b->prime_cap))) return rc;
     // at most prime_cap/32 + one partial chunk per segment (smallest chunk: 32),
     // each as up to 8 n parts
-    if ((rc = b->chunk_seg.ensure(8 * (b->prime_cap / 32 + WAVE_SEGS)))) return rc;
+    if ((rc = b->chunk_seg.ensure(8 * (b->prime_cap / 32 + b->wave_segs)))) return rc;
     if ((rc = b->tot.ensure(8))) return rc;
     if ((rc = b->counters.ensure(4))) return rc;
     if ((rc = b->hits.ensure(1u << 22)) || (rc = b->out.ensure(1u << 20))) return rc;
@@ -980,8 +982,13 @@ int set_chunks(pps_engine* e, uint32_t lo, uint32_t hi, int work) {
 }  // namespace
 
 uint32_t batch_max_slots() { return MAX_JOBS; }
-uint64_t batch_wave_segments() { return WAVE_SEGS; }
+uint64_t batch_wave_segments(const pps_engine* e) {
+  return e && e->batch && e->batch->ready ? e->batch->wave_segs : WAVE_SEGS;
+}
 uint64_t batch_max_piece_span() { return 2ull * SEG_BITS * BATCH_SEGS; }
+uint64_t batch_piece_span(const pps_engine* e) {
+  return 2ull * SEG_BITS * std::min<uint64_t>(BATCH_SEGS, batch_wave_segments(e));
+}
 uint64_t batch_piece_segments(uint64_t lo, uint64_t hi) {
   const uint64_t lo0 = lo | 1ull;
   if (hi <= lo0) return 0;
@@ -1100,8 +1107,8 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
       B.job = pc.slot;
       B.limit = (uint32_t)std::min<uint64_t>(J.qmax, isqrt64(hi - 1));
       const uint32_t ns = (uint32_t)((B.nbits + SEG_BITS - 1) / SEG_BITS);
-      if (nseg + ns > WAVE_SEGS || nb >= WAVE_BATCHES)
-        return set_err(PPS_ERR_INVALID_PARAM, "pieces exceed one wave (%u segments)", WAVE_SEGS);
+      if (nseg + ns > b->wave_segs || nb >= WAVE_BATCHES)
+        return set_err(PPS_ERR_INVALID_PARAM, "pieces exceed one wave (%u segments)", b->wave_segs);
       B.seg0 = nseg;
       for (uint32_t s = 0; s < ns; ++s) {
         BSeg& S = T->seg[nseg + s];
@@ -1297,7 +1304,7 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     return cx > cy;
   });
   std::vector<BatchPiece> pieces;
-  const uint64_t span = batch_max_piece_span();
+  const uint64_t span = batch_piece_span(e);
   for (size_t j : order)
     for (uint64_t lo = jobs[j].pmin | 1ull; lo < jobs[j].pmax; lo += span)
       pieces.push_back(BatchPiece{lo, std::min(jobs[j].pmax, lo + span), (uint32_t)j});
@@ -1310,7 +1317,7 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     size_t z = a;
     while (z < pieces.size() && z - a < WAVE_BATCHES) {
       const uint64_t ns = batch_piece_segments(pieces[z].lo, pieces[z].hi);
-      if (segs + ns > WAVE_SEGS) break;
+      if (segs + ns > b->wave_segs) break;
       segs += ns;
       ++z;
     }
@@ -1367,4 +1374,12 @@ extern "C" int pps_batch_job_primes(pps_engine* e, size_t njobs, uint64_t* prime
   if (!e || !e->batch || !e->batch->ready) return set_err(PPS_ERR_INVALID_PARAM, "no batch has run");
   if (njobs > MAX_JOBS) return set_err(PPS_ERR_INVALID_PARAM, "njobs too large");
   return batch_job_counts(e, 0, njobs, primes, sums);
+}
+
+extern "C" int pps_engine_set_wave_segments(pps_engine* e, uint32_t segments) {
+  if (!e || segments > WAVE_SEGS) return set_err(PPS_ERR_INVALID_PARAM, "wave segments above %u", WAVE_SEGS);
+  if (e->batch && e->batch->ready)
+    return set_err(PPS_ERR_BUSY, "the batched form's buffers are already sized for this engine");
+  e->wave_segs_req = segments;
+  return PPS_OK;
 }

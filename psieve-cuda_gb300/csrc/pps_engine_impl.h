@@ -82,6 +82,7 @@ struct pps_engine {
   // threads per prime of the queued walks: forced (0: tuned), and the tuned
   // choice per (variant set, variant, log2 primes, log2 steps)
   int forced_split = 0;
+  uint32_t wave_segs_req = 0;  // batched form: segments per wave (0: the maximum)
   uint32_t hit_cap_limit = 0;  // the raw-candidate cap of this attempt (0: the buffer's size)
   struct TunedSplit {
     uint64_t mask;
@@ -154,9 +155,10 @@ inline bool batch_hit_less(const pps_hit& x, const pps_hit& y) {  // (slot, p, k
   return x.n < y.n;
 }
 uint32_t batch_max_slots();
-uint64_t batch_wave_segments();          // segments one wave holds
+uint64_t batch_wave_segments(const pps_engine* e);  // segments one wave holds
 uint64_t batch_piece_segments(uint64_t lo, uint64_t hi);
-uint64_t batch_max_piece_span();         // widest p range of one piece
+uint64_t batch_max_piece_span();         // p range of one full batch
+uint64_t batch_piece_span(const pps_engine* e);     // widest p range of one piece on this engine
 int batch_prepare(pps_engine* e);
 // normalised jobs into slots [slot0, slot0 + n); their prime counters start at zero
 int batch_set_jobs(pps_engine* e, uint32_t slot0, const pps_job_params* jobs, size_t n);

@@ -731,6 +731,9 @@ static const VariantTraits kVariants[PPS_NUM_VARIANTS] = {
     {"queue2-bound-u8", true, false, true, false, false, false, true, false, false, 8, 2},
     {"queue-min-u16-r40", true, false, true, false, false, true, false, false, false, 16, 1},
     {"queue-bound-u16-r40", true, false, true, false, false, false, true, false, false, 16, 1},
+    {"queue2-min-u16", true, false, true, false, false, true, false, false, false, 16, 2},
+    {"queue2-min-u8-r64", true, false, true, false, false, true, false, false, false, 8, 2},
+    {"queue2-bound-u16", true, false, true, false, false, false, true, false, false, 16, 2},
 };
 
 const VariantTraits& walk_variant_traits(int v) {
@@ -775,6 +778,9 @@ static walk_fn pick(int v) {
     case 27: return S32 ? k_walk32q2<2, 8, 5> : nullptr;
     case 28: return S32 ? k_walk32q<0, 16, 6> : nullptr;
     case 29: return S32 ? k_walk32q<2, 16, 6> : nullptr;
+    case 30: return S32 ? k_walk32q2<0, 16, 5> : nullptr;
+    case 31: return S32 ? k_walk32q2<0, 8, 4> : nullptr;
+    case 32: return S32 ? k_walk32q2<2, 16, 5> : nullptr;
   }
   return nullptr;
 }

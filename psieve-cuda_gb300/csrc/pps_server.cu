@@ -145,7 +145,7 @@ bool serve_turn(pps_server* s, std::vector<BatchPiece>& pieces, std::vector<pps_
   const double load = std::min(8.0, std::max(1.0, (double)act.size() / 4.0));
   const double work_cap = (double)s->cfg.wave_work * load;
   // a piece is at most one batch, and never more than the wave holds
-  const uint64_t span = std::min<uint64_t>(batch_max_piece_span(), cap * 2ull * pps::SEG_BITS);
+  const uint64_t span = std::min<uint64_t>(batch_piece_span(e), cap * 2ull * pps::SEG_BITS);
   const uint64_t seg_span = 2ull * pps::SEG_BITS;  // p range of one segment
   uint64_t segs = 0;
   double work = 0;
@@ -282,8 +282,8 @@ extern "C" int pps_server_create(int device, const pps_server_config* cfg, pps_s
   if (!c.max_jobs) c.max_jobs = 4096;
   if (c.max_jobs > batch_max_slots())
     return set_err(PPS_ERR_INVALID_PARAM, "max_jobs above %u", batch_max_slots());
-  if (!c.wave_segments || c.wave_segments > batch_wave_segments())
-    c.wave_segments = (uint32_t)batch_wave_segments();
+  if (!c.wave_segments || c.wave_segments > batch_wave_segments(nullptr))
+    c.wave_segments = (uint32_t)batch_wave_segments(nullptr);
   if (!c.wave_work) c.wave_work = 40000000000ull;
   pps_engine* e = nullptr;
   int rc = pps_engine_create(device, &e);

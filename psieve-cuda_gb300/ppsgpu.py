@@ -31,7 +31,7 @@ PPS_ERR_TIMEOUT = -303
 PPS_ERR_BUSY = -304
 PPS_ERR_NOT_FOUND = -305
 PPS_ERR_CANCELLED = -306
-PPS_NUM_VARIANTS = 30
+PPS_NUM_VARIANTS = 33
 TWIN_VARIANTS = (22, 23, 24, 25)  # the walks of both sides of a twin job
 PPS_SIGN_TWIN = 2  # both sides from one walk (the reference's twin build)
 PPS_NOALLOC_MAX_PRIMES = 1 << 24  # per call of pps_check_primes_noalloc
@@ -212,6 +212,7 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_engine_set_batch_span": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
         "pps_engine_set_variant": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
         "pps_engine_set_split": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+        "pps_engine_set_wave_segments": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
         "pps_engine_launches": (ctypes.c_uint64, [ctypes.c_void_p]),
         "pps_run_job": (ctypes.c_int, [ctypes.c_void_p, P(JobParams), ctypes.c_void_p,
                                        ctypes.c_size_t, szp, P(JobStats)]),
@@ -320,6 +321,10 @@ class Engine:
 
     def set_variant(self, v: int) -> None:
         _check(self.lib, self.lib.pps_engine_set_variant(self.h, v))
+
+    def set_wave_segments(self, segments: int) -> None:
+        """Segments per wave of the batched form (before its first use)."""
+        _check(self.lib, self.lib.pps_engine_set_wave_segments(self.h, segments))
 
     def set_split(self, t: int) -> None:
         """Force the threads per prime of the queued walks (1, 2, 4, 8; 0: tuned)."""
