@@ -157,7 +157,7 @@ int pps_engine_sm_count(const pps_engine *e);
 int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 
 /* Force a walk kernel variant (0..PPS_NUM_VARIANTS-1), or -1 for the tuned one. */
-#define PPS_NUM_VARIANTS 33
+#define PPS_NUM_VARIANTS 31
 int pps_engine_set_variant(pps_engine *e, int variant);
 
 /* Force the threads per prime of the queued walks (1, 2, 4 or 8: each prime's

@@ -26,6 +26,7 @@
 
 #include "pps_device.cuh"
 #include "pps_engine_impl.h"
+#include "pps_sieve.cuh"
 
 namespace pps {
 
@@ -294,7 +295,11 @@ __global__ void k_bclear(const uint8_t* tables, uint32_t* bitmap) {
     b4[i] = ones;
 }
 
+// The segment sieve of a wave: as k_sieve_seg (pps_kernels.cu), with the
+// pre-sieve table for 3, 5, 7, 11 and 13 and Barrett reductions (qm) for the
+// start offsets of the small primes.
 __global__ void __launch_bounds__(SIEVE_THREADS) k_bsieve_seg(const uint8_t* tables, const uint32_t* q,
+                                                              const uint64_t* qm, const uint32_t* presieve,
                                                               uint32_t* bitmap, uint32_t* seg_count) {
   __shared__ uint32_t sb[SEG_WORDS];
   __shared__ uint32_t warp_cnt[SIEVE_THREADS / 32];
@@ -310,15 +315,24 @@ __global__ void __launch_bounds__(SIEVE_THREADS) k_bsieve_seg(const uint8_t* tab
   const uint64_t seg_lo = S.lo, seg_hi = seg_lo + 2ull * bits;
   const int have_large = B.nq > B.nq_seg;
   uint32_t* gw = bitmap + (size_t)seg * SEG_WORDS;
+  // pieces start above 2^32, so the pre-sieved primes never lie in a segment
+  const bool pre = presieve != nullptr && B.nq_tiny >= PRESIEVE_PRIMES;
+  const uint32_t xstep = (64u * SIEVE_THREADS) % PRESIEVE_MOD;
+  uint32_t x = pre ? (uint32_t)((seg_lo % PRESIEVE_MOD + 64u * threadIdx.x) % PRESIEVE_MOD) : 0u;
   for (uint32_t w = threadIdx.x; w < SEG_WORDS; w += blockDim.x) {
     uint32_t v = have_large ? gw[w] : 0xffffffffu;
+    if (pre) {
+      v &= ~__ldg(presieve + x);
+      x += xstep;
+      if (x >= PRESIEVE_MOD) x -= PRESIEVE_MOD;
+    }
     const uint32_t j0 = w * 32u;
     if (j0 >= bits) v = 0u;
     else if (bits - j0 < 32u) v &= (1u << (bits - j0)) - 1u;
     sb[w] = v;
   }
   __syncthreads();
-  for (uint32_t i = 0; i < B.nq_tiny; ++i) {
+  for (uint32_t i = pre ? PRESIEVE_PRIMES : 0u; i < B.nq_tiny; ++i) {
     const uint64_t qq = q[i];
     if (qq * qq >= seg_hi) break;
     const uint64_t st = b_first_odd_multiple(qq, seg_lo);
@@ -329,7 +343,14 @@ __global__ void __launch_bounds__(SIEVE_THREADS) k_bsieve_seg(const uint8_t* tab
   for (uint32_t i = B.nq_tiny + threadIdx.x; i < qend; i += blockDim.x) {
     const uint64_t qq = q[i];
     if (qq * qq >= seg_hi) continue;
-    const uint64_t st = b_first_odd_multiple(qq, seg_lo);
+    uint64_t st;
+    if (qq * qq <= seg_lo) {  // the first odd multiple >= seg_lo, by a Barrett reduction
+      const uint64_t r = b_mod(seg_lo, qq, qm[i]);
+      st = r ? seg_lo + (qq - r) : seg_lo;
+      if ((st & 1ull) == 0ull) st += qq;
+    } else {
+      st = b_first_odd_multiple(qq, seg_lo);
+    }
     for (uint64_t j = (st - seg_lo) >> 1; j < bits; j += (uint32_t)qq) atomicAnd(&sb[j >> 5], ~(1u << (j & 31u)));
   }
   __syncthreads();
@@ -377,59 +398,17 @@ __global__ void __launch_bounds__(SIEVE_THREADS) k_bexpand(const uint8_t* tables
                                                            const uint32_t* seg_off, uint64_t* P, uint64_t* Pinv,
                                                            unsigned long long* job_primes,
                                                            unsigned long long* job_sum, uint64_t cap) {
-  constexpr uint32_t WPT = SEG_WORDS / SIEVE_THREADS;
-  __shared__ uint32_t warp_tot[SIEVE_THREADS / 32];
-  __shared__ unsigned long long blk_sum;
+  __shared__ ExpandShared sh;
   const WaveTables* T = wt(tables);
   const uint32_t seg = blockIdx.x;
   if (seg >= T->nseg) return;
   const BSeg S = T->seg[seg];
   const uint32_t job = T->batch[S.batch].job;
-  const uint32_t* gw = bitmap + (size_t)seg * SEG_WORDS + threadIdx.x * WPT;
-  const uint64_t base_val = S.lo + 2ull * (threadIdx.x * WPT * 32u);
-  uint32_t w[WPT];
-  uint32_t c = 0;
-#pragma unroll
-  for (uint32_t i = 0; i < WPT; ++i) {
-    w[i] = gw[i];
-    c += __popc(w[i]);
-  }
-  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-  uint32_t inc = c;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= (uint32_t)o) inc += v;
-  }
-  if (lane == 31) warp_tot[wid] = inc;
-  if (threadIdx.x == 0) blk_sum = 0ull;
-  __syncthreads();
-  uint32_t woff = 0;
-  for (uint32_t i = 0; i < wid; ++i) woff += warp_tot[i];
-  uint64_t pos = (uint64_t)seg_off[seg] + woff + inc - c;
-  uint64_t sum = 0;
-#pragma unroll
-  for (uint32_t i = 0; i < WPT; ++i) {
-    uint32_t v = w[i];
-    while (v) {
-      const uint32_t bit = __ffs(v) - 1u;
-      v &= v - 1u;
-      const uint64_t p = base_val + 2ull * (i * 32u + bit);
-      sum += p;
-      if (pos < cap) {
-        P[pos] = p;
-        Pinv[pos] = neg_inv64(p);
-      }
-      ++pos;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-  if (lane == 0) atomicAdd(&blk_sum, (unsigned long long)sum);
-  __syncthreads();
+  const uint64_t sum = expand_segment<false>(bitmap + (size_t)seg * SEG_WORDS, S.lo, seg_off[seg], cap, P, Pinv,
+                                             nullptr, &sh);
   if (threadIdx.x == 0) {
-    uint32_t tot = 0;
-    for (uint32_t i = 0; i < (SIEVE_THREADS >> 5); ++i) tot += warp_tot[i];
-    atomicAdd(&job_primes[job], (unsigned long long)tot);
-    atomicAdd(&job_sum[job], blk_sum);
+    atomicAdd(&job_primes[job], (unsigned long long)sh.total);
+    atomicAdd(&job_sum[job], (unsigned long long)sum);
   }
 }
 
@@ -830,7 +809,8 @@ int launch_wave_sieve(pps_engine* e, const uint32_t* dq, uint32_t nq_all) {
   CU(cudaMemsetAsync(b->counters.p + 3, 0, sizeof(uint32_t), st));
   k_bsieve_large<<<e->num_sms * 8, 256, 0, st>>>(b->tables.p, dq, b->qm.p, b->bitmap.p, b->large_off.p,
                                                  b->tot.p + 4, b->counters.p + 3);
-  k_bsieve_seg<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, dq, b->bitmap.p, b->seg_count.p);
+  k_bsieve_seg<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, dq, b->qm.p, e->presieve.p, b->bitmap.p,
+                                                     b->seg_count.p);
   k_bscan<<<1, 1024, 0, st>>>(b->seg_count.p, b->seg_off.p, WAVE_SEGS, b->tot.p);
   k_bexpand<<<WAVE_SEGS, SIEVE_THREADS, 0, st>>>(b->tables.p, b->bitmap.p, b->seg_off.p, b->P.p, b->Pinv.p,
                                                   b->job_primes.p, b->job_sum.p, b->prime_cap);

@@ -170,6 +170,8 @@ static void free_engine(pps_engine* e) {
   e->factors.release();
   e->counters.release();
   e->small_q.release();
+  e->presieve.release();
+  e->sieve_res.release();
   e->probe_sink.release();
   batch_state_free(e);
   if (e->h_pinned) cudaFreeHost(e->h_pinned);
@@ -221,6 +223,12 @@ extern "C" int pps_engine_create(int device, pps_engine** out) {
     e->nsmall = (uint32_t)sp16.size();
     if ((rc = e->small_q.ensure(sp16.size()))) break;
     if (cudaMemcpy(e->small_q.p, sp16.data(), sp16.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "copy"); break; }
+    {
+      std::vector<uint32_t> pre(PRESIEVE_WORDS);
+      presieve_table(pre.data());
+      if ((rc = e->presieve.ensure(PRESIEVE_WORDS))) break;
+      if (cudaMemcpy(e->presieve.p, pre.data(), PRESIEVE_WORDS * 4, cudaMemcpyHostToDevice) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "copy"); break; }
+    }
     e->host_seed = host_odd_primes(SEG_BITS - 1);
     if ((rc = e->seed_q.ensure(e->host_seed.size()))) break;
     if (cudaMemcpy(e->seed_q.p, e->host_seed.data(), e->host_seed.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) { rc = set_err(PPS_ERR_CUDA, "copy"); break; }
@@ -239,7 +247,8 @@ extern "C" uint64_t pps_engine_device_bytes(const pps_engine* e) {
   if (!e) return 0;
   return e->base_q.bytes() + e->seed_q.bytes() + e->bitmap.bytes() + e->seg_count.bytes() +
          e->seg_off.bytes() + e->P.bytes() + e->Pinv.bytes() + e->totals.bytes() + e->hits.bytes() +
-         e->factors.bytes() + e->counters.bytes() + e->small_q.bytes() + e->probe_sink.bytes();
+         e->factors.bytes() + e->counters.bytes() + e->small_q.bytes() + e->probe_sink.bytes() +
+         e->presieve.bytes() + e->sieve_res.bytes();
 }
 
 extern "C" int pps_engine_sm_count(const pps_engine* e) { return e ? e->num_sms : 0; }
@@ -293,6 +302,12 @@ static int sieve_batch(pps_engine* e, uint64_t lo, uint64_t hi, const uint32_t* 
   b.seg_count = e->seg_count.p;
   b.seg_off = e->seg_off.p;
   b.d_total = e->totals.p;
+  b.presieve = e->presieve.p;
+  // residues in 32 bits need seg * (2 SEG_BITS mod q) + (lo mod q) < 2^32
+  if (nq_seg > nq_tiny && b.nseg <= 8192u) {
+    if ((rc = e->sieve_res.ensure(2 * (size_t)(nq_seg - nq_tiny)))) return rc;
+    b.res = e->sieve_res.p;
+  }
   CU(cudaMemsetAsync(e->totals.p, 0, 2 * sizeof(uint64_t), e->st));
   e->launches += launch_sieve_batch(b, out64, pinv64, out32, e->st);
   CU(cudaGetLastError());
@@ -506,7 +521,7 @@ static int run_walk(pps_engine* e, const pps_job_params* jp, int v, const uint64
   a.hits = e->hits.p;
   a.hit_count = e->counters.p;
   a.hit_cap = hit_cap_now(e);
-  const int threads = 256;
+  const int threads = walk_block_threads(v);
   int maxb = walk_max_blocks(v, threads, jp->step, e->num_sms);
   if (maxb <= 0) return set_err(PPS_ERR_CUDA, "walk variant %d unavailable", v);
   // queued walks: a warp covers 32 x per_thread primes of one n part
@@ -606,7 +621,7 @@ static int autotune(pps_engine* e, const pps_job_params* jp, const uint64_t* dP,
   // pass rates): a choice is reused only within the same set
   // a forced variant is honoured only where it is exact for this job
   if (e->forced_variant >= 0 && variant_ok(jp, e->forced_variant) &&
-      walk_max_blocks(e->forced_variant, 256, jp->step, e->num_sms) > 0)
+      walk_max_blocks(e->forced_variant, walk_block_threads(e->forced_variant), jp->step, e->num_sms) > 0)
     return e->forced_variant;
   const uint64_t sample = std::min<uint64_t>(np, (uint64_t)e->num_sms * 8 * 256);
   // long enough that per-prime setup and launch timing do not sway the comparison

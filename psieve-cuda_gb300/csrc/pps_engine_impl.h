@@ -107,6 +107,8 @@ struct pps_engine {
   DevBuf<pps_factor> factors;
   DevBuf<uint32_t> counters;  // [0] raw hits, [1] factors
   DevBuf<uint16_t> small_q;
+  DevBuf<uint32_t> presieve;  // the pre-sieve table for 3, 5, 7, 11, 13 (PRESIEVE_WORDS)
+  DevBuf<uint32_t> sieve_res; // per-batch residues of the small sieving primes
   uint32_t nsmall = 0;
   DevBuf<uint32_t> probe_sink;
   uint64_t* h_pinned = nullptr;  // 16 words of pinned host scratch

@@ -30,7 +30,20 @@ struct SieveBatch {
   uint32_t* seg_count;
   uint32_t* seg_off;  // exclusive scan of seg_count
   uint64_t* d_total;  // [0] = primes in batch (written by scan), [1] = wrapping sum
+  // optional: the pre-sieve table (PRESIEVE_WORDS words: bit b of word x set
+  // when the value x + 2b (mod PRESIEVE_MOD) has a factor 3, 5, 7, 11 or 13),
+  // replacing the marking by those five primes; and per-batch residues of the
+  // sieving primes q[nq_tiny .. nq_seg): res[2i] = lo mod q, res[2i+1] =
+  // 2 SEG_BITS mod q, so a segment's start offsets need no 64-bit division
+  const uint32_t* presieve = nullptr;
+  uint32_t* res = nullptr;
 };
+
+constexpr uint32_t PRESIEVE_MOD = 3u * 5u * 7u * 11u * 13u;  // 15015
+constexpr uint32_t PRESIEVE_WORDS = PRESIEVE_MOD;
+constexpr uint32_t PRESIEVE_PRIMES = 5;  // 3, 5, 7, 11, 13: the first five sieving primes
+// The pre-sieve table (host side, to copy to the device once).
+void presieve_table(uint32_t* out);
 
 // Launch the full sieve of one batch on `st`: large-prime scatter, segment
 // sieve, scan, expansion into out64 (+ Montgomery constants into pinv64 when
@@ -108,6 +121,8 @@ int set_error_text(int code, const char* msg);
 // Largest useful grid for the walk kernel of variant v with `threads` threads
 // per block (occupancy-derived); 0 if the variant cannot run this step size.
 int walk_max_blocks(int v, int threads, uint32_t step, int num_sms);
+// Threads per block of variant v's launch.
+int walk_block_threads(int v);
 cudaError_t launch_walk(int v, const WalkArgs& a, int blocks, int threads, cudaStream_t st);
 
 // ----------------------------------------------------------------- filter

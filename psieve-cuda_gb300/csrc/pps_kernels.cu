@@ -21,6 +21,7 @@
 
 #include "pps_device.cuh"
 #include "pps_internal.h"
+#include "pps_sieve.cuh"
 
 namespace pps {
 
@@ -51,6 +52,26 @@ __global__ void k_sieve_large(SieveBatch b) {
   }
 }
 
+void presieve_table(uint32_t* out) {
+  for (uint32_t x = 0; x < PRESIEVE_MOD; ++x) {
+    uint32_t m = 0;
+    for (uint32_t bit = 0; bit < 32; ++bit) {
+      const uint32_t v = (x + 2u * bit) % PRESIEVE_MOD;
+      if (v % 3u == 0 || v % 5u == 0 || v % 7u == 0 || v % 11u == 0 || v % 13u == 0) m |= 1u << bit;
+    }
+    out[x] = m;
+  }
+}
+
+// Per-batch residues of the small sieving primes (see SieveBatch::res).
+__global__ void k_sieve_res(SieveBatch b) {
+  for (uint32_t i = b.nq_tiny + blockIdx.x * blockDim.x + threadIdx.x; i < b.nq_seg; i += gridDim.x * blockDim.x) {
+    const uint32_t q = b.q[i];
+    b.res[2 * (i - b.nq_tiny)] = (uint32_t)(b.lo % q);
+    b.res[2 * (i - b.nq_tiny) + 1] = (2u * SEG_BITS) % q;
+  }
+}
+
 __global__ void __launch_bounds__(SIEVE_THREADS) k_sieve_seg(SieveBatch b, int have_large) {
   __shared__ uint32_t sb[SEG_WORDS];
   __shared__ uint32_t warp_cnt[SIEVE_THREADS / 32];
@@ -61,18 +82,37 @@ __global__ void __launch_bounds__(SIEVE_THREADS) k_sieve_seg(SieveBatch b, int h
   const uint64_t seg_lo = b.lo + 2ull * seg_first;
   const uint64_t seg_hi = seg_lo + 2ull * bits;
   uint32_t* gw = b.bitmap + (size_t)seg * SEG_WORDS;
+  // the pre-sieve table's entry for word w is at (seg_lo + 64 w) mod 15015
+  const bool pre = b.presieve != nullptr && b.nq_tiny >= PRESIEVE_PRIMES;
+  const uint32_t x0 = pre ? (uint32_t)(seg_lo % PRESIEVE_MOD) : 0u;
+  const uint32_t xstep = (64u * SIEVE_THREADS) % PRESIEVE_MOD;
+  uint32_t x = pre ? (x0 + 64u * threadIdx.x) % PRESIEVE_MOD : 0u;
 
   for (uint32_t w = threadIdx.x; w < SEG_WORDS; w += blockDim.x) {
     uint32_t v = have_large ? gw[w] : 0xffffffffu;
+    if (pre) {
+      v &= ~__ldg(b.presieve + x);
+      x += xstep;
+      if (x >= PRESIEVE_MOD) x -= PRESIEVE_MOD;
+    }
     const uint32_t j0 = w * 32u;
     if (j0 >= bits) v = 0u;
     else if (bits - j0 < 32u) v &= (1u << (bits - j0)) - 1u;
     sb[w] = v;
   }
   __syncthreads();
+  if (pre && seg_lo <= 13u && threadIdx.x == 0) {
+    // the five pre-sieved primes themselves are primes
+    for (uint32_t q = 3; q <= 13; q += 2)
+      if (q != 9 && q >= seg_lo && q < seg_hi) {
+        const uint32_t j = (uint32_t)((q - seg_lo) >> 1);
+        sb[j >> 5] |= 1u << (j & 31u);
+      }
+  }
+  __syncthreads();
 
   // tiny primes: the CTA strides one q at a time
-  for (uint32_t i = 0; i < b.nq_tiny; ++i) {
+  for (uint32_t i = pre ? PRESIEVE_PRIMES : 0; i < b.nq_tiny; ++i) {
     const uint64_t q = b.q[i];
     if (q * q >= seg_hi) break;
     const uint64_t st = first_odd_multiple(q, seg_lo);
@@ -85,10 +125,18 @@ __global__ void __launch_bounds__(SIEVE_THREADS) k_sieve_seg(SieveBatch b, int h
   for (uint32_t i = b.nq_tiny + threadIdx.x; i < qend; i += blockDim.x) {
     const uint64_t q = b.q[i];
     if (q * q >= seg_hi) continue;
-    const uint64_t st = first_odd_multiple(q, seg_lo);
     const uint32_t qq = (uint32_t)q;
-    for (uint64_t j = (st - seg_lo) >> 1; j < bits; j += qq)
-      atomicAnd(&sb[j >> 5], ~(1u << (j & 31u)));
+    uint32_t j;
+    if (b.res != nullptr && q * q <= seg_lo) {
+      // seg_lo mod q from the batch's residues, in 32 bits (seg < 2^13, q < 2^18)
+      const uint32_t r = (b.res[2 * (i - b.nq_tiny)] + b.res[2 * (i - b.nq_tiny) + 1] * seg) % qq;
+      uint32_t d = r ? qq - r : 0u;  // seg_lo + d is the first multiple of q >= seg_lo
+      if (d & 1u) d += qq;           // seg_lo is odd: the odd multiple
+      j = d >> 1;
+    } else {
+      j = (uint32_t)((first_odd_multiple(q, seg_lo) - seg_lo) >> 1);
+    }
+    for (; j < bits; j += qq) atomicAnd(&sb[j >> 5], ~(1u << (j & 31u)));
   }
   __syncthreads();
 
@@ -133,63 +181,27 @@ __global__ void __launch_bounds__(1024) k_scan_counts(const uint32_t* cnt, uint3
   if (threadIdx.x == blockDim.x - 1) d_total[0] = part[threadIdx.x];
 }
 
-// One CTA per segment: rank the set bits and write the primes in order.
+// One CTA per segment: rank the set bits and write the primes in order
+// (expand_segment, pps_sieve.cuh).
 template <bool OUT32>
 __global__ void __launch_bounds__(SIEVE_THREADS) k_expand(SieveBatch b, uint64_t* out64, uint64_t* pinv64,
                                                           uint32_t* out32) {
-  constexpr uint32_t WPT = SEG_WORDS / SIEVE_THREADS;  // words per thread
-  __shared__ uint32_t warp_tot[SIEVE_THREADS / 32];
-  __shared__ unsigned long long blk_sum;
+  __shared__ ExpandShared sh;
   const uint32_t seg = blockIdx.x;
-  const uint32_t* gw = b.bitmap + (size_t)seg * SEG_WORDS + threadIdx.x * WPT;
-  const uint64_t base_val = b.lo + 2ull * ((uint64_t)seg * SEG_BITS + threadIdx.x * WPT * 32u);
-  uint32_t w[WPT];
-  uint32_t c = 0;
-#pragma unroll
-  for (uint32_t i = 0; i < WPT; ++i) {
-    w[i] = gw[i];
-    c += __popc(w[i]);
-  }
-  // block exclusive scan of c
-  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-  uint32_t inc = c;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= (uint32_t)o) inc += v;
-  }
-  if (lane == 31) warp_tot[wid] = inc;
-  if (threadIdx.x == 0) blk_sum = 0ull;
-  __syncthreads();
-  uint32_t woff = 0;
-  for (uint32_t i = 0; i < wid; ++i) woff += warp_tot[i];
-  uint64_t pos = (uint64_t)b.seg_off[seg] + woff + inc - c;
-  uint64_t sum = 0;
-#pragma unroll
-  for (uint32_t i = 0; i < WPT; ++i) {
-    uint32_t v = w[i];
-    while (v) {
-      const uint32_t bit = __ffs(v) - 1u;
-      v &= v - 1u;
-      const uint64_t p = base_val + 2ull * (i * 32u + bit);
-      sum += p;
-      if (OUT32) {
-        out32[pos] = (uint32_t)p;
-      } else {
-        out64[pos] = p;
-        if (pinv64) pinv64[pos] = neg_inv64(p);
-      }
-      ++pos;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-  if (lane == 0) atomicAdd(&blk_sum, (unsigned long long)sum);
-  __syncthreads();
-  if (threadIdx.x == 0) atomicAdd((unsigned long long*)&b.d_total[1], blk_sum);
+  const uint64_t sum = expand_segment<OUT32>(b.bitmap + (size_t)seg * SEG_WORDS,
+                                             b.lo + 2ull * (uint64_t)seg * SEG_BITS, b.seg_off[seg], ~0ull,
+                                             out64, pinv64, out32, &sh);
+  if (threadIdx.x == 0) atomicAdd((unsigned long long*)&b.d_total[1], (unsigned long long)sum);
 }
 
 int launch_sieve_batch(const SieveBatch& b, uint64_t* out64, uint64_t* pinv64, uint32_t* out32,
                        cudaStream_t st) {
   int launches = 0;
+  if (b.res && b.nq_seg > b.nq_tiny) {
+    const uint32_t n = b.nq_seg - b.nq_tiny;
+    k_sieve_res<<<(n + 255) / 256, 256, 0, st>>>(b);
+    ++launches;
+  }
   const int have_large = b.nq > b.nq_seg;
   if (have_large) {
     cudaMemsetAsync(b.bitmap, 0xff, (size_t)b.nseg * SEG_WORDS * sizeof(uint32_t), st);
@@ -731,8 +743,6 @@ static const VariantTraits kVariants[PPS_NUM_VARIANTS] = {
     {"queue2-bound-u8", true, false, true, false, false, false, true, false, false, 8, 2},
     {"queue-min-u16-r40", true, false, true, false, false, true, false, false, false, 16, 1},
     {"queue-bound-u16-r40", true, false, true, false, false, false, true, false, false, 16, 1},
-    {"queue2-min-u16", true, false, true, false, false, true, false, false, false, 16, 2},
-    {"queue2-min-u8-r64", true, false, true, false, false, true, false, false, false, 8, 2},
     {"queue2-bound-u16", true, false, true, false, false, false, true, false, false, 16, 2},
 };
 
@@ -778,11 +788,14 @@ static walk_fn pick(int v) {
     case 27: return S32 ? k_walk32q2<2, 8, 5> : nullptr;
     case 28: return S32 ? k_walk32q<0, 16, 6> : nullptr;
     case 29: return S32 ? k_walk32q<2, 16, 6> : nullptr;
-    case 30: return S32 ? k_walk32q2<0, 16, 5> : nullptr;
-    case 31: return S32 ? k_walk32q2<0, 8, 4> : nullptr;
-    case 32: return S32 ? k_walk32q2<2, 16, 5> : nullptr;
+    case 30: return S32 ? k_walk32q2<2, 16, 5> : nullptr;
   }
   return nullptr;
+}
+
+int walk_block_threads(int v) {
+  (void)v;
+  return 256;
 }
 
 int walk_max_blocks(int v, int threads, uint32_t step, int num_sms) {

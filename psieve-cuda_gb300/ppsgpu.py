@@ -31,7 +31,7 @@ PPS_ERR_TIMEOUT = -303
 PPS_ERR_BUSY = -304
 PPS_ERR_NOT_FOUND = -305
 PPS_ERR_CANCELLED = -306
-PPS_NUM_VARIANTS = 33
+PPS_NUM_VARIANTS = 31
 TWIN_VARIANTS = (22, 23, 24, 25)  # the walks of both sides of a twin job
 PPS_SIGN_TWIN = 2  # both sides from one walk (the reference's twin build)
 PPS_NOALLOC_MAX_PRIMES = 1 << 24  # per call of pps_check_primes_noalloc
