@@ -321,7 +321,9 @@ def run_other_workloads(eng) -> dict:
         dt = time.perf_counter() - t0
         out[name] = {"primes": int(st.primes), "seconds": dt, "primes_per_s": st.primes / dt,
                      "n_steps_per_s": st.steps / dt, "factors": len(fac), "nstep": int(jp.nstep),
-                     "walk_step": int(jp.step), "variant": int(st.variant), "split": int(st.split)}
+                     "walk_step": int(jp.step), "variant": int(st.variant), "split": int(st.split),
+                     "phase_ms": {"sieve": st.sieve_ms, "walk": st.walk_ms, "filter": st.filter_ms,
+                                  "device_total": st.total_ms}}
     # Few primes, long n: p in [4.2e13, 4.2e13 + 2e6) holds 63,903 primes, about
     # a quarter of a wave of the walk's resident threads.  The chosen threads
     # per prime against one thread per prime (forced), each timed after a

@@ -344,6 +344,7 @@ static int ensure_base(pps_engine* e, uint32_t limit, BaseTable* bt) {
     // the table is rebuilt from scratch: a failure below leaves no table
     e->base_limit = 0;
     e->base_count = 0;
+    e->base_le.clear();
     if ((rc = e->base_q.ensure(cap))) return rc;
     uint64_t filled = 0;
     const uint64_t span = 1ull << 31;
@@ -359,18 +360,24 @@ static int ensure_base(pps_engine* e, uint32_t limit, BaseTable* bt) {
     e->base_limit = limit;
     e->base_count = (uint32_t)filled;
   }
-  // counts for `limit` within the (possibly larger) table
+  // counts for `limit` within the (possibly larger) table: a binary search on
+  // the device values through small copies, remembered per limit until the
+  // table is rebuilt
   uint32_t n = e->base_count;
   if (e->base_limit > limit) {
-    // binary search on device values through small copies
-    uint32_t lo = 0, hi = e->base_count;  // find first index with q > limit
-    while (lo < hi) {
-      uint32_t mid = lo + (hi - lo) / 2;
-      uint32_t v;
-      CU(cudaMemcpy(&v, e->base_q.p + mid, 4, cudaMemcpyDeviceToHost));
-      if (v <= limit) lo = mid + 1; else hi = mid;
+    auto it = e->base_le.find(limit);
+    if (it != e->base_le.end()) {
+      n = it->second;
+    } else {
+      // the first index with q > limit, by a binary search on the device
+      uint32_t* d_n = (uint32_t*)(e->totals.p + 2);  // a free word of the totals
+      CU(launch_count_le(e->base_q.p, e->base_count, limit, d_n, e->st));
+      e->launches++;
+      CU(cudaMemcpyAsync(e->h_pinned, d_n, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
+      CU(cudaStreamSynchronize(e->st));
+      n = ((uint32_t*)e->h_pinned)[0];
+      e->base_le[limit] = n;
     }
-    n = lo;
   }
   bt->nq = n;
   bt->nq_tiny = std::min(n, count_le(e->host_seed, TINY_Q_LIMIT - 1));
@@ -746,16 +753,11 @@ extern "C" int pps_engine_set_input(pps_engine* e, const pps_input* in) {
 }
 
 // Filter the raw hits accumulated in e->hits and copy the factors out.
+// The filter runs on the device-side count of raw hits (clamped to the
+// buffer), so the two counts come back in one copy after it: a raw count
+// beyond the buffer then means an overflow (the call walks again).
 static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, size_t cap, size_t* nout,
                       pps_job_stats* st, uint32_t* raw_hits_out, bool* overflow) {
-  CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
-  CU(cudaStreamSynchronize(e->st));
-  const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
-  *raw_hits_out = raw;
-  if (raw > hit_cap_now(e)) {
-    *overflow = true;
-    return PPS_OK;
-  }
   if (int rc = ensure_input_keys(e, jp)) return rc;
   FilterArgs f;
   f.hits = e->hits.p;
@@ -779,13 +781,18 @@ static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, 
     f.kmax = jp->kmax;
   }
   CU(cudaEventRecord(e->ev[4], e->st));
-  if (raw) {
-    CU(launch_filter(f, raw, e->st));
-    e->launches++;
-  }
+  // a grid of a few resident waves; the kernel reads the count on the device
+  CU(launch_filter(f, (uint32_t)e->num_sms * 64u, e->st));
+  e->launches++;
   CU(cudaEventRecord(e->ev[5], e->st));
   CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
   CU(cudaStreamSynchronize(e->st));
+  const uint32_t raw = ((uint32_t*)e->h_pinned)[0];
+  *raw_hits_out = raw;
+  if (raw > hit_cap_now(e)) {
+    *overflow = true;
+    return PPS_OK;
+  }
   const uint32_t nf = ((uint32_t*)e->h_pinned)[1];
   float fms = 0;
   CU(cudaEventElapsedTime(&fms, e->ev[4], e->ev[5]));

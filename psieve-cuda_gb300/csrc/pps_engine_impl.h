@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <vector>
 
 #include "pps_internal.h"
@@ -97,6 +98,7 @@ struct pps_engine {
   DevBuf<uint32_t> base_q;
   uint32_t base_limit = 0;
   uint32_t base_count = 0;
+  std::map<uint32_t, uint32_t> base_le;  // primes <= limit in the table, per limit asked
   std::vector<uint32_t> host_seed;  // odd primes < SEG_BITS (host copy)
   DevBuf<uint32_t> seed_q;
 

@@ -51,6 +51,9 @@ void presieve_table(uint32_t* out);
 int launch_sieve_batch(const SieveBatch& b, uint64_t* out64, uint64_t* pinv64, uint32_t* out32,
                        cudaStream_t st);
 
+// Number of entries <= x of the ascending table q[0..n), into *out (one thread).
+cudaError_t launch_count_le(const uint32_t* q, uint32_t n, uint32_t x, uint32_t* out, cudaStream_t st);
+
 // ------------------------------------------------------------------- walk
 struct WalkArgs {
   const uint64_t* P;        // primes

@@ -194,6 +194,20 @@ __global__ void __launch_bounds__(SIEVE_THREADS) k_expand(SieveBatch b, uint64_t
   if (threadIdx.x == 0) atomicAdd((unsigned long long*)&b.d_total[1], (unsigned long long)sum);
 }
 
+__global__ void k_count_le(const uint32_t* q, uint32_t n, uint32_t x, uint32_t* out) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (q[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  *out = lo;
+}
+
+cudaError_t launch_count_le(const uint32_t* q, uint32_t n, uint32_t x, uint32_t* out, cudaStream_t st) {
+  k_count_le<<<1, 1, 0, st>>>(q, n, x, out);
+  return cudaGetLastError();
+}
+
 int launch_sieve_batch(const SieveBatch& b, uint64_t* out64, uint64_t* pinv64, uint32_t* out32,
                        cudaStream_t st) {
   int launches = 0;
