@@ -141,10 +141,10 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def _traffic_from_profile() -> float | None:
-    """DRAM bytes per prime of the walk kernel from the committed ncu summary
-    (the walk reads each prime's 16 B once, whatever the n range)."""
-    f = ROOT / "profiles" / "k_walk32q_large_n.md"
+def _traffic_from_profile(kernel: str) -> float | None:
+    """DRAM bytes per prime of the walk kernel from the committed ncu summary of
+    that kernel (the walk reads each prime's 16 B once, whatever the n range)."""
+    f = ROOT / "profiles" / f"{kernel}_large_n.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -264,6 +264,10 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
     t0 = time.perf_counter()
     per, bst = eng.run_batch(jobs)
     t_batch = time.perf_counter() - t0
+    # the plain form again, its tuner now warm for every kind of job in the mix
+    t0 = time.perf_counter()
+    plain_warm = [eng.run_job(jp)[0] for jp in jobs]
+    t_plain_warm = time.perf_counter() - t0
     # where the time goes: device time per phase, the rest is host turns
     # (launches, syncs, copies, tuning) and, for the plain form, the tuner's runs
     sieve = sum(x.sieve_ms for x in pst)
@@ -288,7 +292,8 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
     for c in classes.values():
         c["walk_steps_per_s"] = c["steps"] / (c["walk_ms"] * 1e-3) if c["walk_ms"] else None
     breakdown["plain_by_kind"] = classes
-    identical = len(per) == len(plain) and all(np.array_equal(a, b) for a, b in zip(per, plain))
+    identical = (len(per) == len(plain) == len(plain_warm) and
+                 all(np.array_equal(a, b) and np.array_equal(a, c) for a, b, c in zip(per, plain, plain_warm)))
     job_primes, job_sums = eng.batch_job_primes(len(jobs))
     checked = {"jobs": jobs, "lists": per, "job_primes": job_primes, "job_sums": job_sums}
     return checked, {"workload": f"{count} mixed jobs, seed {seed} (the mixed-job distribution); {repaired} "
@@ -297,7 +302,11 @@ def run_mixed(eng, count: int = 512, seed: int = 1) -> dict:
             "plain_s": t_plain, "batched_s": t_batch,
             "plain_primes_per_s": plain_primes / t_plain, "batched_primes_per_s": bst.primes / t_batch,
             "speedup": t_plain / t_batch, "identical_results": bool(identical),
+            "plain_warm_s": t_plain_warm, "speedup_vs_warm_plain": t_plain_warm / t_batch,
+            "plain_note": "plain_s: one pps_run_job per job, the walk tuner timing each new kind of job "
+                          "as it meets it; plain_warm_s: the same jobs again with every kind tuned",
             "waves": int(bst.waves), "chunk": int(bst.chunk), "unroll": int(bst.unroll),
+            "primes_per_lane": int(bst.primes_per_lane),
             "batched_n_steps_per_s": bst.steps / t_batch, "breakdown": breakdown}
 
 
@@ -728,17 +737,18 @@ def run_gpu(args) -> None:
     peak_mults = eng.imad_peak()
     mults = 3.0 * steps_done
     achieved = mults / (walk_ms * 1e-3)
-    traffic = _traffic_from_profile()
+    variant = stats[-1].variant if stats else 0
+    kernel = ppsgpu.walk_kernel_name(variant)
+    traffic = _traffic_from_profile(kernel)
     peaks = _measured_peaks()
     hbm = peaks.get("hbm_gbs")
     sieve_gbs = 16.0 * primes / (sieve_ms * 1e-3) / 1e9 if sieve_ms > 0 else None
     launches_walk = len(stats)  # one walk launch per job
-    variant = stats[-1].variant if stats else 0
     roofline = {"bound": "imad", "achieved": achieved / 1e9, "peak": peak_mults / 1e9,
                 "unit": "Gmul/s", "frac": achieved / peak_mults,
                 "traffic": (traffic * primes / launches_walk) if traffic else None,
                 "traffic_unit": "bytes per launch (ncu DRAM bytes per prime x primes per launch)",
-                "kernel": f"{'k_walk32q' if variant >= 10 else 'k_walk'} (variant {variant})",
+                "kernel": f"{kernel} (variant {variant}: {ppsgpu.walk_variant_name(variant)})",
                 "peak_source": "measured in this run (pps_measure_imad_peak)",
                 "work_per_unit": "3 multiplies per walk step (one prime advanced by 32 n)",
                 "sieve": {"bound": "hbm", "achieved": sieve_gbs, "peak": hbm, "unit": "GB/s",

@@ -160,6 +160,10 @@ int pps_engine_set_batch_span(pps_engine *e, uint64_t span);
 #define PPS_NUM_VARIANTS 31
 int pps_engine_set_variant(pps_engine *e, int variant);
 
+/* A walk variant's short description ("queue2-min-u8": queued walk, two primes
+   per thread, running-minimum window, 8-step blocks), or "?" out of range. */
+const char *pps_walk_variant_name(int variant);
+
 /* Force the threads per prime of the queued walks (1, 2, 4 or 8: each prime's
    n range is cut into that many parts walked side by side), or 0 for the
    choice per job (where a job's primes fill less than one wave of the walk's
@@ -255,7 +259,8 @@ int pps_engine_set_input(pps_engine *e, const pps_input *in);
    exactly as pps_run_job would return them. */
 typedef struct {
   uint64_t primes, prime_sum, raw_hits, factors, steps;
-  uint32_t waves, chunk, unroll, pad;
+  uint32_t waves, chunk, unroll;
+  uint32_t primes_per_lane;  /* the tuned walk: 2 where 32-bit-step jobs walk two primes per lane */
   double total_ms, filter_ms;
   double sieve_ms, walk_ms;  /* device time of the waves' sieve parts and walks */
 } pps_batch_stats;

@@ -639,16 +639,125 @@ __device__ __forceinline__ void b_round(const BJob& J, uint32_t job, uint32_t pa
   __syncwarp();
 }
 
-template <int U>
-__global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, const BJob* jobs,
+// Two primes per lane (32-bit steps, one side, hi-word windows or the single
+// bound): the same walk and queue as b_round for FORM 0, with lane l walking
+// primes l and 32 + l of the round side by side (two independent step chains);
+// queue entries carry the prime's slot (0..63) in their top 6 bits.
+template <int U, int TEST>
+__device__ __forceinline__ void b_round2(const BJob& J, uint32_t job, uint32_t part, uint64_t p0, uint64_t ps0,
+                                         bool v0, uint64_t p1, uint64_t ps1, bool v1, uint32_t* qe, uint32_t* qc,
+                                         uint64_t* qp, uint64_t* qk, uint32_t qcap, pps_hit* hits,
+                                         uint32_t* hit_count, uint32_t hit_cap) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nsteps = J.nsteps, full = nsteps / (uint32_t)U;
+  const uint32_t nsplit = J.nsplit > 1u ? J.nsplit : 1u;
+  const uint32_t per = (full + nsplit - 1u) / nsplit;
+  const uint32_t b_lo = min(full, part * per), b_hi = min(full, b_lo + per);
+  const bool last_part = part == nsplit - 1u;
+  const uint32_t tag = job | (J.proth == 1u ? SIDE_PROTH : 0u);
+  qp[lane] = p0;
+  qp[32 + lane] = p1;
+  if (v0) {
+    const uint32_t pa0 = neg_lo(p0), pb0 = neg_hi(p0), pi0 = lo32(ps0);
+    const uint32_t pa1 = neg_lo(p1), pb1 = neg_hi(p1), pi1 = lo32(ps1);
+    const uint32_t n0 = J.nmin + 32u * (uint32_t)U * b_lo;
+    const uint64_t x0 = inv_pow2(n0, p0, ps0), x1 = inv_pow2(n0, p1, ps1);
+    const uint64_t K0 = J.proth == 1u ? p0 - x0 : x0, K1 = J.proth == 1u ? p1 - x1 : x1;
+    uint32_t klo0 = lo32(K0), khi0 = hi32(K0), klo1 = lo32(K1), khi1 = hi32(K1);
+    const uint32_t win_mask = J.win_mask, win_u = J.win_u, bound_hi = J.bound_hi;
+    for (uint32_t b = b_lo; b < b_hi; ++b) {
+      uint32_t acc0 = 0xffffffffu, acc1 = 0xffffffffu;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (TEST == 0) {
+          acc0 = min(acc0, min(__funnelshift_rc(khi0, 0u, win_u), klo0 & win_mask));
+          acc1 = min(acc1, min(__funnelshift_rc(khi1, 0u, win_u), klo1 & win_mask));
+        } else if (TEST == 3) {
+          acc0 = min(acc0, min(khi0, klo0 & win_mask));
+          acc1 = min(acc1, min(khi1, klo1 & win_mask));
+        } else {
+          acc0 = min(acc0, khi0);
+          acc1 = min(acc1, khi1);
+        }
+        step_neg32(klo0, khi0, pa0, pb0, pi0);
+        step_neg32(klo1, khi1, pa1, pb1, pi1);
+      }
+      const bool f0 = TEST == 2 ? acc0 <= bound_hi : acc0 == 0u;
+      const bool f1 = v1 && (TEST == 2 ? acc1 <= bound_hi : acc1 == 0u);
+      if (f0 | f1) {
+        const uint32_t pos = atomicAdd(qc, (uint32_t)f0 + (uint32_t)f1);
+        if (f0 && pos < qcap) qe[pos] = (lane << 26) | b;
+        if (f1 && pos + (uint32_t)f0 < qcap) qe[pos + (uint32_t)f0] = ((32u + lane) << 26) | b;
+      }
+    }
+    if (last_part && full * (uint32_t)U < nsteps) {
+      qk[lane] = mk64(klo0, khi0);
+      qk[32 + lane] = mk64(klo1, khi1);
+      const uint32_t pos = atomicAdd(qc, 1u + (uint32_t)v1);
+      if (pos < qcap) qe[pos] = (lane << 26) | full;
+      if (v1 && pos + 1u < qcap) qe[pos + 1u] = ((32u + lane) << 26) | full;
+    }
+  }
+  __syncwarp();
+  const uint32_t cnt = *qc;
+  if (cnt <= qcap) {
+    for (uint32_t e = lane; e < cnt; e += 32u) {
+      const uint32_t ent = qe[e];
+      const uint32_t owner = ent >> 26, blk = ent & ((1u << 26) - 1u);
+      const uint64_t op = qp[owner];
+      const uint64_t ops = neg_inv64(op);
+      const uint32_t t0 = (uint32_t)U * blk;
+      const uint32_t nblk = min((uint32_t)U, nsteps - t0);
+      const uint32_t n0 = J.nmin + 32u * t0;
+      uint64_t K;
+      if (blk == full) {
+        K = qk[owner];
+      } else {
+        const uint64_t x = inv_pow2(n0, op, ops);
+        K = J.proth == 1u ? op - x : x;
+      }
+      uint32_t klo = lo32(K), khi = hi32(K);
+      const uint32_t opa = neg_lo(op), opb = neg_hi(op), opinv = lo32(ops);
+#pragma unroll 1
+      for (uint32_t u = 0; u < nblk; ++u) {
+        b_record(klo, khi, n0 + 32u * u, 32u, op, tag, J, hits, hit_count, hit_cap);
+        step_neg32(klo, khi, opa, opb, opinv);
+      }
+    }
+  } else {
+    // queue overflow: the exact test at every step of this part, both primes
+    for (int which = 0; which < 2; ++which) {
+      if (which ? !v1 : !v0) continue;
+      const uint64_t p = which ? p1 : p0, ps = which ? ps1 : ps0;
+      const uint32_t pa = neg_lo(p), pb = neg_hi(p), pinv = lo32(ps);
+      const uint32_t t_lo = (uint32_t)U * b_lo, t_hi = last_part ? nsteps : (uint32_t)U * b_hi;
+      const uint64_t x = inv_pow2(J.nmin + 32u * t_lo, p, ps);
+      const uint64_t K = J.proth == 1u ? p - x : x;
+      uint32_t klo = lo32(K), khi = hi32(K);
+#pragma unroll 1
+      for (uint32_t t = t_lo; t < t_hi; ++t) {
+        b_record(klo, khi, J.nmin + 32u * t, 32u, p, tag, J, hits, hit_count, hit_cap);
+        step_neg32(klo, khi, pa, pb, pinv);
+      }
+    }
+  }
+  __syncwarp();
+  if ((threadIdx.x & 31u) == 0) *qc = 0;
+  __syncwarp();
+}
+
+// TWO: rounds of the eligible jobs walk two primes per lane (b_round2); the
+// kernel then holds 64 registers a thread (4 CTAs per SM) instead of 48 (5).
+template <int U, bool TWO>
+__global__ void __launch_bounds__(BW_THREADS, TWO ? 4 : 5) k_bwalk(const uint8_t* tables, const BJob* jobs,
                                                          const uint32_t* seg_count, const uint32_t* seg_off,
                                                          const uint32_t* chunk_off, const uint32_t* chunk_seg,
                                                          const uint64_t* P, const uint64_t* Pinv, uint64_t* tot,
                                                          uint64_t chunk_limit, uint32_t qcap, pps_hit* hits,
                                                          uint32_t* hit_count, uint32_t hit_cap) {
   __shared__ uint32_t q_ent[BW_THREADS / 32][BQ_CAP];
-  __shared__ uint64_t q_p[BW_THREADS / 32][32];
-  __shared__ uint64_t q_k[BW_THREADS / 32][32];
+  __shared__ uint64_t q_p[BW_THREADS / 32][64];
+  __shared__ uint64_t q_k[BW_THREADS / 32][64];
   __shared__ uint32_t q_cnt[BW_THREADS / 32];
   const WaveTables* T = wt(tables);
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
@@ -671,7 +780,26 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
     const uint32_t within = (w / nsplit) * J.chunk;
     const uint32_t count = min(J.chunk, seg_count[s] - within);
     const uint64_t first = (uint64_t)seg_off[s] + within;
-    for (uint32_t r = 0; r < count; r += 32u) {
+    // two primes per lane where the job's steps are 32 n with a hi-word window
+    // or the single bound, and more than one warp's worth of primes remain
+    const bool two = TWO && J.step == 32 && J.proth != 2u && J.win_sh >= 32u;
+    for (uint32_t r = 0; r < count;) {
+      if (two && count - r > 32u) {
+        const bool v1 = r + 32u + lane < count;
+        const uint64_t pi0 = first + r + lane, pi1 = first + r + 32u + (v1 ? lane : 0u);
+        const uint64_t p0 = P[pi0], ps0 = Pinv[pi0], p1 = P[pi1], ps1 = Pinv[pi1];
+        if (J.bound_hi != 0xffffffffu)
+          b_round2<U, 2>(J, job, part, p0, ps0, true, p1, ps1, v1, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib],
+                         qcap, hits, hit_count, hit_cap);
+        else if (J.win_u == 0u)
+          b_round2<U, 3>(J, job, part, p0, ps0, true, p1, ps1, v1, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib],
+                         qcap, hits, hit_count, hit_cap);
+        else
+          b_round2<U, 0>(J, job, part, p0, ps0, true, p1, ps1, v1, q_ent[wib], &q_cnt[wib], q_p[wib], q_k[wib],
+                         qcap, hits, hit_count, hit_cap);
+        r += 64u;
+        continue;
+      }
       const bool valid = r + lane < count;
       const uint64_t pi = first + r + (valid ? lane : 0u);
       const uint64_t p = P[pi], ps = Pinv[pi];
@@ -695,6 +823,7 @@ __global__ void __launch_bounds__(BW_THREADS, 5) k_bwalk(const uint8_t* tables, 
       else PPS_BROUND_F(2);
 #undef PPS_BROUND_F
 #undef PPS_BROUND
+      r += 32u;
     }
   }
 }
@@ -823,12 +952,24 @@ int launch_wave_sieve(pps_engine* e, const uint32_t* dq, uint32_t nq_all) {
   return PPS_OK;
 }
 
+// The walk kernel of a tuning code: the unroll (8 or 16) plus WALK_TWO for two
+// primes per lane.
+constexpr int WALK_TWO = 0x100;
+typedef void (*bwalk_fn)(const uint8_t*, const BJob*, const uint32_t*, const uint32_t*, const uint32_t*,
+                         const uint32_t*, const uint64_t*, const uint64_t*, uint64_t*, uint64_t, uint32_t,
+                         pps_hit*, uint32_t*, uint32_t);
+bwalk_fn bwalk_kernel(int code) {
+  const bool two = (code & WALK_TWO) != 0;
+  if ((code & 0xff) == 16) return two ? k_bwalk<16, true> : k_bwalk<16, false>;
+  return two ? k_bwalk<8, true> : k_bwalk<8, false>;
+}
+
 int launch_wave_walk(pps_engine* e, int unroll, uint64_t chunk_limit, pps_hit* hits, uint32_t* hit_count,
                      uint32_t hit_cap) {
   BatchState* b = e->batch;
   cudaStream_t st = e->st;
   int per_sm = 0;
-  auto fn = unroll == 16 ? k_bwalk<16> : k_bwalk<8>;
+  auto fn = bwalk_kernel(unroll);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
   const int grid = (per_sm > 0 ? per_sm : 1) * e->num_sms;
   fn<<<grid, BW_THREADS, 0, st>>>(b->tables.p, b->jobs.p, b->seg_count.p, b->seg_off.p, b->chunk_off.p,
@@ -928,8 +1069,10 @@ void chunk_for(BJob* J, int work, int forced_split) {
   if (forced_split > 0) t = (uint32_t)forced_split;
   const uint64_t per = (nsteps + t - 1) / t;
   const uint64_t c = ((uint64_t)work * 32u / per + 31u) & ~31ull;
+  // jobs the walk may take two primes per lane for get at least 64 (a round of two)
+  const uint64_t cmin = J->step == 32 && J->proth != 2u && J->win_sh >= 32u ? 64 : 32;
   J->nsplit = t;
-  J->chunk = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, 32), MAX_CHUNK);
+  J->chunk = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(c, cmin), MAX_CHUNK);
 }
 
 // Copy mirror slots [lo, hi) to the device.  The source is pageable: the call
@@ -988,7 +1131,7 @@ int batch_prepare(pps_engine* e) {
 void batch_tuning(pps_engine* e, uint32_t* work, uint32_t* unroll) {
   const BatchState* b = e ? e->batch : nullptr;
   if (work) *work = b ? (uint32_t)b->tuned_work : 0;
-  if (unroll) *unroll = b ? (uint32_t)b->tuned_unroll : 0;
+  if (unroll) *unroll = b ? (uint32_t)b->tuned_unroll & 0xffu : 0;
 }
 
 int batch_set_jobs(pps_engine* e, uint32_t slot0, const pps_job_params* jobs, size_t n) {
@@ -1117,10 +1260,10 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
   };
 
   if (!b->tuned_work) {
-    // time each (work per chunk, unroll) on the first chunks of this wave,
-    // the same number of walk steps for every candidate
+    // time each (work per chunk, unroll, one or two primes per lane) on the
+    // first chunks of this wave, the same number of walk steps for every candidate
     const int works[] = {256, 1024, 4096};
-    const int unrolls[] = {8, 16};
+    const int unrolls[] = {8, 16, 8 | WALK_TWO, 16 | WALK_TWO};
     float best = 1e30f;
     for (int w : works)
       for (int u : unrolls) {
@@ -1132,7 +1275,7 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
           return rc;
         CU(cudaEventRecord(e->ev[0], st));
         CU(cudaMemsetAsync(b->tot.p + 3, 0, sizeof(uint64_t), st));
-        auto fn = u == 16 ? k_bwalk<16> : k_bwalk<8>;
+        auto fn = bwalk_kernel(u);
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BW_THREADS, 0);
         fn<<<std::max(per_sm, 1) * e->num_sms, BW_THREADS, 0, st>>>(
@@ -1338,7 +1481,8 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     bst->factors = nf;
     bst->waves = (uint32_t)waves;
     bst->chunk = (uint32_t)b->tuned_work;
-    bst->unroll = (uint32_t)b->tuned_unroll;
+    bst->unroll = (uint32_t)b->tuned_unroll & 0xffu;
+    bst->primes_per_lane = (b->tuned_unroll & WALK_TWO) ? 2u : 1u;
     float ms = 0;
     CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
     bst->total_ms = ms;

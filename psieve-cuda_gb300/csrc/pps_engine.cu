@@ -274,6 +274,8 @@ extern "C" int pps_engine_set_split(pps_engine* e, int split) {
 
 extern "C" uint64_t pps_engine_launches(const pps_engine* e) { return e ? e->launches : 0; }
 
+extern "C" const char* pps_walk_variant_name(int v) { return walk_variant_name(v); }
+
 // ----------------------------------------------------------------- sieve
 uint32_t isqrt64(uint64_t x) {
   uint64_t r = (uint64_t)sqrt((double)x);

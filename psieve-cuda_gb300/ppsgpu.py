@@ -79,7 +79,7 @@ class BatchStats(ctypes.Structure):
                 ("raw_hits", ctypes.c_uint64), ("factors", ctypes.c_uint64),
                 ("steps", ctypes.c_uint64), ("waves", ctypes.c_uint32),
                 ("chunk", ctypes.c_uint32), ("unroll", ctypes.c_uint32),
-                ("pad", ctypes.c_uint32), ("total_ms", ctypes.c_double),
+                ("primes_per_lane", ctypes.c_uint32), ("total_ms", ctypes.c_double),
                 ("filter_ms", ctypes.c_double), ("sieve_ms", ctypes.c_double),
                 ("walk_ms", ctypes.c_double)]
 
@@ -212,6 +212,7 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_engine_set_batch_span": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
         "pps_engine_set_variant": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
         "pps_engine_set_split": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+        "pps_walk_variant_name": (ctypes.c_char_p, [ctypes.c_int]),
         "pps_engine_set_wave_segments": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
         "pps_engine_launches": (ctypes.c_uint64, [ctypes.c_void_p]),
         "pps_run_job": (ctypes.c_int, [ctypes.c_void_p, P(JobParams), ctypes.c_void_p,
@@ -271,6 +272,21 @@ def normalize(pmin=0, pmax=0, kmin=0, kmax=0, nmin=0, nmax=0, sign=1, kstep=0, k
     out = JobParams()
     _check(lib, lib.pps_normalize(ctypes.byref(spec), ctypes.byref(out)))
     return out
+
+
+def walk_variant_name(v: int, lib=None) -> str:
+    """The walk variant's short description (pps_walk_variant_name)."""
+    return (lib or load()).pps_walk_variant_name(v).decode()
+
+
+def walk_kernel_name(v: int, lib=None) -> str:
+    """The CUDA kernel that runs walk variant v."""
+    name = walk_variant_name(v, lib)
+    if name.startswith("queue2"):
+        return "k_walk32q2"
+    if name.startswith(("queue", "twin")):
+        return "k_walk32q"
+    return "k_walk"
 
 
 def format_line(p: int, k: int, n: int, c: int) -> str:

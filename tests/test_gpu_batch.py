@@ -34,6 +34,7 @@ def test_batch_equals_single_jobs_mixed(pps, engine):
         total += len(want)
     assert st.factors == total
     assert st.waves >= 1 and st.chunk in (256, 1024, 4096) and st.unroll in (8, 16)
+    assert st.primes_per_lane in (1, 2)
 
 
 def test_batch_repeat_and_degenerate(pps, engine, ora):

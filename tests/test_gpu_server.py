@@ -139,3 +139,25 @@ def test_server_cancel_queued_and_running(pps, engine):
     want, wst = engine.run_job(small)
     assert pps.factors_to_tuples(fac) == pps.factors_to_tuples(want) and res.primes == wst.primes
     assert st.failed == 2 and st.running == 0 and st.queued == 0
+
+
+def test_server_small_job_overtakes_a_long_one(pps, engine):
+    """Waves are cut by walk work: a small job submitted while a long job is
+    being walked joins the next wave and finishes long before it, with its
+    exact list; the long job's list is exact too."""
+    import time
+
+    long_job = pps.normalize(pmin=42 * 10**12, pmax=42 * 10**12 + 3 * 10**9, kmin=1201, kmax=9999,
+                             nmin=2000000, nmax=3000000)  # about 3e12 walk steps, over a second of the GPU
+    small = pps.normalize(pmin=10**12, pmax=10**12 + 10**6, kmin=1201, kmax=9999, nmin=2000, nmax=3000)
+    with pps.Server(0, wave_work=2 * 10**10) as srv:
+        jl = srv.submit(long_job)
+        time.sleep(0.05)  # the long job is in its first waves
+        js = srv.submit(small)
+        fs, rs = srv.wait(js)
+        assert srv.poll(jl) == pps.PPS_JOB_RUNNING
+        fl, rl = srv.wait(jl)
+    assert rs.latency_ms < rl.latency_ms / 5
+    for fac, jp in ((fs, small), (fl, long_job)):
+        want, _ = engine.run_job(jp)
+        assert pps.factors_to_tuples(fac) == pps.factors_to_tuples(want)
