@@ -111,7 +111,8 @@ struct BatchState {
   uint32_t graph_hcap = 0, graph_qcap = 0;  // candidate and warp-queue capacities it was captured with
   cudaEvent_t copied = nullptr;
   uint32_t wave_segs = WAVE_SEGS;  // segments one wave holds (pps_engine_set_wave_segments)
-  int tuned_work = 0, tuned_unroll = 0;  // walk steps per chunk (x32 lanes), inner unroll
+  int tuned_work = 0, tuned_unroll = 0;  // walk steps per chunk (x32 lanes), walk kernel code (timed)
+  int walk_code = 0;                     // the walk kernel code of the last wave (tuned or forced)
   std::vector<BJob> hjobs;               // host mirror of the device job slots
   std::vector<uint64_t> slot_pmax;       // each slot's pmax (sieving-prime bound)
   DevBuf<unsigned long long> bak_primes, bak_sum;  // slot counters before a wave
@@ -1131,7 +1132,7 @@ int batch_prepare(pps_engine* e) {
 void batch_tuning(pps_engine* e, uint32_t* work, uint32_t* unroll) {
   const BatchState* b = e ? e->batch : nullptr;
   if (work) *work = b ? (uint32_t)b->tuned_work : 0;
-  if (unroll) *unroll = b ? (uint32_t)b->tuned_unroll & 0xffu : 0;
+  if (unroll) *unroll = b ? (uint32_t)b->walk_code & 0xffu : 0;
 }
 
 int batch_set_jobs(pps_engine* e, uint32_t slot0, const pps_job_params* jobs, size_t n) {
@@ -1305,6 +1306,8 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
       }
     if ((rc = restore())) return rc;
   }
+  // the walk kernel of this wave: the tuner's, unless pps_engine_set_batch_walk forces one
+  b->walk_code = e->forced_bwalk ? e->forced_bwalk : b->tuned_unroll;
   if ((rc = set_chunks(e, smin, smax, b->tuned_work))) return rc;
 
   // the wave itself: a captured graph of the fixed sequence, replayed
@@ -1315,7 +1318,7 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
   if (debug_first_hit_cap() && debug_first_hit_cap() < hcap) hcap = debug_first_hit_cap();
   for (;;) {
     const uint32_t qcap = std::min(debug_queue_cap(), BQ_CAP);
-    if (!b->graph || !b->graph_walk || b->graph_unroll != b->tuned_unroll || b->graph_q != dq ||
+    if (!b->graph || !b->graph_walk || b->graph_unroll != b->walk_code || b->graph_q != dq ||
         b->graph_nq != nq_all || b->graph_hcap != hcap || b->graph_qcap != qcap) {
       drop_graphs(b);
       for (int part = 0; part < 2; ++part) {
@@ -1323,7 +1326,7 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
         CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         const uint64_t launches0 = e->launches;
         rc = part == 0 ? launch_wave_sieve(e, dq, nq_all)
-                       : launch_wave_walk(e, b->tuned_unroll, 0, b->hits.p, b->counters.p, hcap);
+                       : launch_wave_walk(e, b->walk_code, 0, b->hits.p, b->counters.p, hcap);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         e->launches = launches0;
         if (rc) return rc;
@@ -1335,7 +1338,7 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
           return set_err(PPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
         }
       }
-      b->graph_unroll = b->tuned_unroll;
+      b->graph_unroll = b->walk_code;
       b->graph_q = dq;
       b->graph_nq = nq_all;
       b->graph_hcap = hcap;
@@ -1481,8 +1484,8 @@ extern "C" int pps_run_batch(pps_engine* e, const pps_job_params* jobs, size_t n
     bst->factors = nf;
     bst->waves = (uint32_t)waves;
     bst->chunk = (uint32_t)b->tuned_work;
-    bst->unroll = (uint32_t)b->tuned_unroll & 0xffu;
-    bst->primes_per_lane = (b->tuned_unroll & WALK_TWO) ? 2u : 1u;
+    bst->unroll = (uint32_t)b->walk_code & 0xffu;
+    bst->primes_per_lane = (b->walk_code & WALK_TWO) ? 2u : 1u;
     float ms = 0;
     CU(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
     bst->total_ms = ms;
@@ -1505,5 +1508,17 @@ extern "C" int pps_engine_set_wave_segments(pps_engine* e, uint32_t segments) {
   if (e->batch && e->batch->ready)
     return set_err(PPS_ERR_BUSY, "the batched form's buffers are already sized for this engine");
   e->wave_segs_req = segments;
+  return PPS_OK;
+}
+
+extern "C" int pps_engine_set_batch_walk(pps_engine* e, int unroll, int primes_per_lane) {
+  if (!e) return set_err(PPS_ERR_INVALID_PARAM, "null engine");
+  if (unroll == 0 && primes_per_lane == 0) {
+    e->forced_bwalk = 0;
+    return PPS_OK;
+  }
+  if ((unroll != 8 && unroll != 16) || (primes_per_lane != 1 && primes_per_lane != 2))
+    return set_err(PPS_ERR_INVALID_PARAM, "batched walk: unroll 8 or 16, 1 or 2 primes per lane");
+  e->forced_bwalk = unroll | (primes_per_lane == 2 ? WALK_TWO : 0);
   return PPS_OK;
 }

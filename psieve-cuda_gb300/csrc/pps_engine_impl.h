@@ -84,6 +84,7 @@ struct pps_engine {
   // choice per (variant set, variant, log2 primes, log2 steps)
   int forced_split = 0;
   uint32_t wave_segs_req = 0;  // batched form: segments per wave (0: the maximum)
+  int forced_bwalk = 0;        // batched form: forced walk kernel code (0: tuned)
   uint32_t hit_cap_limit = 0;  // the raw-candidate cap of this attempt (0: the buffer's size)
   struct TunedSplit {
     uint64_t mask;

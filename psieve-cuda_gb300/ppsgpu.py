@@ -212,6 +212,7 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
         "pps_engine_set_batch_span": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
         "pps_engine_set_variant": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
         "pps_engine_set_split": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+        "pps_engine_set_batch_walk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
         "pps_walk_variant_name": (ctypes.c_char_p, [ctypes.c_int]),
         "pps_engine_set_wave_segments": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
         "pps_engine_launches": (ctypes.c_uint64, [ctypes.c_void_p]),
@@ -341,6 +342,10 @@ class Engine:
     def set_wave_segments(self, segments: int) -> None:
         """Segments per wave of the batched form (before its first use)."""
         _check(self.lib, self.lib.pps_engine_set_wave_segments(self.h, segments))
+
+    def set_batch_walk(self, unroll: int, primes_per_lane: int) -> None:
+        """Force the batched walk kernel (8 or 16, 1 or 2); (0, 0): tuned."""
+        _check(self.lib, self.lib.pps_engine_set_batch_walk(self.h, unroll, primes_per_lane))
 
     def set_split(self, t: int) -> None:
         """Force the threads per prime of the queued walks (1, 2, 4, 8; 0: tuned)."""

@@ -57,6 +57,24 @@ def test_batch_repeat_and_degenerate(pps, engine, ora):
     assert per == [] and st.factors == 0
 
 
+@pytest.mark.parametrize("unroll,lanes", [(8, 1), (16, 1), (8, 2), (16, 2)])
+def test_batch_walk_kernels_match_reference(pps, engine, ref_cases, unroll, lanes):
+    """Each batched walk kernel (8- or 16-step blocks, one or two primes per lane
+    for the 32-bit-step jobs), forced: every list is the reference's."""
+    names = sorted(k for k in ref_cases if k.startswith("rand"))
+    extra = ["large_n_slice0", "large_n_slice3", "riesel62_slice_lo", "small_proth_full"]
+    names += extra
+    jobs = [pps.normalize(**args_to_spec(ref_cases[n]["args"])) for n in names]
+    engine.set_batch_walk(unroll, lanes)
+    try:
+        per, st = engine.run_batch(jobs)
+    finally:
+        engine.set_batch_walk(0, 0)
+    assert (st.unroll, st.primes_per_lane) == (unroll, lanes)
+    for j, name in enumerate(names):
+        assert lines_of(pps.factors_to_tuples(per[j])) == sorted(set(ref_cases[name]["lines"])), name
+
+
 @pytest.mark.parametrize("split", [2, 8])
 def test_batch_n_parts_match_oracle(pps, engine, ora, ref_cases, split):
     """Each job's n range cut into `split` parts, each part its own work item
@@ -71,10 +89,12 @@ def test_batch_n_parts_match_oracle(pps, engine, ora, ref_cases, split):
     ]
     jobs += [pps.normalize(**s) for s in extra]
     engine.set_split(split)
+    engine.set_batch_walk(16, 2)  # the two-primes-per-lane walk over the n parts too
     try:
         per, _ = engine.run_batch(jobs)
     finally:
         engine.set_split(0)
+        engine.set_batch_walk(0, 0)
     for j, name in enumerate(names):
         assert lines_of(pps.factors_to_tuples(per[j])) == sorted(set(ref_cases[name]["lines"])), name
     for i, spec in enumerate(extra):
