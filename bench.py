@@ -712,6 +712,8 @@ def run_gpu(args) -> None:
         barrier()
         h2d = d2h = 0
         e_primes = 0
+        e_walk_ms = 0.0
+        e_variants = set()
         e2e_lists = []
         t0 = time.perf_counter()
         for i in range(args.warmup, need):
@@ -721,11 +723,15 @@ def run_gpu(args) -> None:
             h2d += pin.numel() * 8
             d2h += 8 + fac.nbytes
             e_primes += st.primes
+            e_walk_ms += st.walk_ms
+            e_variants.add(int(st.variant))
         barrier()
         e_el = max_over_ranks(time.perf_counter() - t0)
         e2e = {"value": sum_over_ranks(e_primes) / e_el, "unit": "primes/s",
                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
-               "path": "pps_check_primes (host primes in pinned memory -> factors to host)"}
+               "path": "pps_check_primes (host primes in pinned memory -> factors to host)",
+               "ms_per_step": 1e3 * e_el / args.steps, "walk_ms_per_step": e_walk_ms / args.steps,
+               "variants": sorted(e_variants)}
         del host_sets
 
     if rank != 0:

@@ -830,40 +830,19 @@ __global__ void __launch_bounds__(BW_THREADS, TWO ? 4 : 5) k_bwalk(const uint8_t
 }
 
 // output rule per candidate with its job's parameters
-__global__ void k_bfilter(const pps_hit* hits, const uint32_t* d_nhits, uint32_t hit_cap, const BJob* jobs,
-                          const uint16_t* small_q, uint32_t nsmall, pps_hit* out, uint32_t* out_count,
-                          uint32_t out_cap) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+__global__ void __launch_bounds__(FILTER_THREADS) k_bfilter(const pps_hit* hits, const uint32_t* d_nhits,
+                                                            uint32_t hit_cap, const BJob* jobs,
+                                                            const uint16_t* small_q, uint32_t nsmall, pps_hit* out,
+                                                            uint32_t* out_count, uint32_t out_cap) {
   uint32_t nh = *d_nhits;
   if (nh > hit_cap) nh = hit_cap;
-  for (uint32_t h = warp; h < nh; h += nwarps) {
+  for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
     const pps_hit x = hits[h];
     const BJob J = jobs[x.idx & ~SIDE_PROTH];
     const int32_t c = (x.idx & SIDE_PROTH) ? 1 : -1;
     bool ok = (x.k == J.kstep * (x.k / J.kstep) + J.koffset) && x.n >= J.nmin && x.n < J.nmax;
-    if (ok) {
-      bool div = false;
-      for (uint32_t base = 0; base < nsmall; base += 32u) {
-        const uint32_t i = base + lane;
-        if (i < nsmall) {
-          const uint32_t q = small_q[i];
-          const uint32_t kr = (uint32_t)(x.k % q);
-          uint32_t r = 1u, b = 2u % q, e = x.n;
-          while (e) {
-            if (e & 1u) r = (r * b) % q;
-            b = (b * b) % q;
-            e >>= 1;
-          }
-          const uint32_t t = (kr * r) % q;
-          div = ((t + (uint32_t)((int32_t)q + c)) % q) == 0u;
-        }
-        if (__any_sync(0xffffffffu, div)) break;
-      }
-      ok = !__any_sync(0xffffffffu, div);
-    }
-    if (ok && lane == 0) {
+    if (ok) ok = !cta_small_factor(x.k, x.n, c, small_q, nsmall);  // the same in every thread
+    if (ok && threadIdx.x == 0) {
       const uint32_t pos = atomicAdd(out_count, 1u);
       if (pos < out_cap) out[pos] = x;
     }
@@ -1377,10 +1356,9 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
     uint32_t nf = 0;
     for (;;) {
       CU(cudaMemsetAsync(b->counters.p + 1, 0, sizeof(uint32_t), st));
-      uint32_t blocks = (raw * 32u + 255u) / 256u;
-      if (blocks > 4096u) blocks = 4096u;
-      k_bfilter<<<blocks, 256, 0, st>>>(b->hits.p, b->counters.p, (uint32_t)b->hits.n, b->jobs.p, e->small_q.p,
-                                        e->nsmall, b->out.p, b->counters.p + 1, (uint32_t)b->out.n);
+      k_bfilter<<<filter_blocks(raw), FILTER_THREADS, 0, st>>>(b->hits.p, b->counters.p, (uint32_t)b->hits.n,
+                                                               b->jobs.p, e->small_q.p, e->nsmall, b->out.p,
+                                                               b->counters.p + 1, (uint32_t)b->out.n);
       CU(cudaGetLastError());
       e->launches++;
       CU(cudaMemcpyAsync(e->h_pinned, b->counters.p + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));

@@ -189,4 +189,33 @@ __device__ __forceinline__ void step_form2(uint32_t& klo, uint32_t& khi, uint32_
   khi = hi32(r);
 }
 
+// ---------------------------------------------------------------- output rule
+// Whether the odd prime q < 2^16 divides k 2^n + c (c = +-1): the trial
+// division of pps/factor_proth.c:247-253 by the primes below 32768, in 32-bit
+// arithmetic (every product of two residues stays below 2^32).
+__device__ __forceinline__ bool small_divides(uint64_t k, uint32_t n, int32_t c, uint32_t q) {
+  const uint32_t t32 = (0xffffffffu % q + 1u) % q;  // 2^32 mod q
+  const uint32_t kr = ((hi32(k) % q) * t32 + lo32(k) % q) % q;
+  uint32_t r = 1u, b = 2u;
+  for (uint32_t e = n; e; e >>= 1) {
+    if (e & 1u) r = r * b % q;
+    b = b * b % q;
+  }
+  return (kr * r + (uint32_t)((int32_t)q + c)) % q == 0u;
+}
+
+// Whether k 2^n + c has a factor among small_q[0, nsmall), tested by all the
+// threads of a CTA together: rounds of blockDim.x primes, ending with the
+// first round that finds one.  Every thread of the CTA calls it with the same
+// arguments.
+__device__ __forceinline__ bool cta_small_factor(uint64_t k, uint32_t n, int32_t c, const uint16_t* small_q,
+                                                 uint32_t nsmall) {
+  for (uint32_t base = 0; base < nsmall; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const bool d = i < nsmall && small_divides(k, n, c, small_q[i]);
+    if (__syncthreads_or(d)) return true;
+  }
+  return false;
+}
+
 }  // namespace pps

@@ -783,8 +783,9 @@ static int finish_job(pps_engine* e, const pps_job_params* jp, pps_factor* out, 
     f.kmax = jp->kmax;
   }
   CU(cudaEventRecord(e->ev[4], e->st));
-  // a grid of a few resident waves; the kernel reads the count on the device
-  CU(launch_filter(f, (uint32_t)e->num_sms * 64u, e->st));
+  // one resident wave of CTAs (one per candidate at a time); the kernel reads
+  // the count on the device
+  CU(launch_filter(f, (uint32_t)e->num_sms * 8u, e->st));
   e->launches++;
   CU(cudaEventRecord(e->ev[5], e->st));
   CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));

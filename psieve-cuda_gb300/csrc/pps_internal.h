@@ -148,6 +148,12 @@ struct FilterArgs {
   uint64_t kmin = 0, kmax = 0;
 };
 cudaError_t launch_filter(const FilterArgs& a, uint32_t max_hits, cudaStream_t st);
+// The filters run one CTA of FILTER_THREADS per candidate, over a grid of at
+// most FILTER_MAX_BLOCKS that loops over the device-side count.
+constexpr uint32_t FILTER_THREADS = 256, FILTER_MAX_BLOCKS = 2048;
+inline uint32_t filter_blocks(uint32_t max_hits) {
+  return max_hits == 0 ? 1u : (max_hits < FILTER_MAX_BLOCKS ? max_hits : FILTER_MAX_BLOCKS);
+}
 
 // ------------------------------------------------------------- utilities
 cudaError_t launch_imad_probe(uint32_t* sink, uint32_t iters, int blocks, int threads,

@@ -829,29 +829,19 @@ cudaError_t launch_walk(int v, const WalkArgs& a, int blocks, int threads, cudaS
 
 // ==================================================================== filter
 
-__device__ __forceinline__ uint32_t pow2_mod_small(uint32_t e, uint32_t q) {
-  uint32_t r = 1u, b = 2u % q;
-  while (e) {
-    if (e & 1u) r = (r * b) % q;
-    b = (b * b) % q;
-    e >>= 1;
-  }
-  return r;
-}
-
-__global__ void k_filter(FilterArgs a) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+// The output rule on the raw candidates, one CTA per candidate (its threads
+// share the trial division, so that a candidate that survives it, the one
+// that takes all 3,512 primes, costs 14 rounds of 256 instead of 110 of 32).
+__global__ void __launch_bounds__(FILTER_THREADS) k_filter(FilterArgs a) {
   uint32_t nh = *a.d_nhits;
   if (nh > a.hit_cap) nh = a.hit_cap;
-  for (uint32_t h = warp; h < nh; h += nwarps) {
+  for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
     const pps_hit x = a.hits[h];
     // a twin job's candidates say their side; every other job has one
     const int32_t c = a.sign == PPS_SIGN_TWIN ? ((x.idx & HIT_SIDE_PROTH) ? 1 : -1) : a.sign;
     bool ok = (x.k == a.kstep * (x.k / a.kstep) + a.koffset) && x.n >= a.nmin && x.n < a.nmax;
     if (ok && a.in_keys) {
-      // the input file's bit of (k, n), every lane the same search
+      // the input file's bit of (k, n), every thread the same search
       ok = x.k >= a.kmin && x.k <= a.kmax;
       if (ok) {
         const uint64_t key = (uint64_t)(x.n - a.nmin) * a.in_width + (x.k - a.kmin) / a.kstep;
@@ -863,20 +853,9 @@ __global__ void k_filter(FilterArgs a) {
         ok = lo < a.in_n && a.in_keys[lo] == key;
       }
     } else if (ok) {
-      bool div = false;
-      for (uint32_t base = 0; base < a.nsmall; base += 32u) {
-        const uint32_t i = base + lane;
-        if (i < a.nsmall) {
-          const uint32_t q = a.small_q[i];
-          const uint32_t kr = (uint32_t)(x.k % q);
-          const uint32_t t = (kr * pow2_mod_small(x.n, q)) % q;
-          div = ((t + (uint32_t)((int32_t)q + c)) % q) == 0u;
-        }
-        if (__any_sync(0xffffffffu, div)) break;
-      }
-      ok = !__any_sync(0xffffffffu, div);
+      ok = !cta_small_factor(x.k, x.n, c, a.small_q, a.nsmall);  // ok is the same in every thread
     }
-    if (ok && lane == 0) {
+    if (ok && threadIdx.x == 0) {
       const uint32_t pos = atomicAdd(a.out_count, 1u);
       if (pos < a.out_cap) {
         pps_factor f;
@@ -891,10 +870,8 @@ __global__ void k_filter(FilterArgs a) {
 }
 
 cudaError_t launch_filter(const FilterArgs& a, uint32_t max_hits, cudaStream_t st) {
-  uint32_t warps = max_hits ? max_hits : 1u;
-  uint32_t blocks = (warps * 32u + 255u) / 256u;
-  if (blocks > 4096u) blocks = 4096u;
-  k_filter<<<blocks, 256, 0, st>>>(a);
+  const uint32_t blocks = filter_blocks(max_hits);
+  k_filter<<<blocks, FILTER_THREADS, 0, st>>>(a);
   return cudaGetLastError();
 }
 
