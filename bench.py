@@ -729,7 +729,8 @@ def run_gpu(args) -> None:
         e_el = max_over_ranks(time.perf_counter() - t0)
         e2e = {"value": sum_over_ranks(e_primes) / e_el, "unit": "primes/s",
                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
-               "path": "pps_check_primes (host primes in pinned memory -> factors to host)",
+               "path": "pps_check_primes (host primes in pinned memory, read in place by the walk over the "
+                       "host link -> factors to host)",
                "ms_per_step": 1e3 * e_el / args.steps, "walk_ms_per_step": e_walk_ms / args.steps,
                "variants": sorted(e_variants)}
         del host_sets

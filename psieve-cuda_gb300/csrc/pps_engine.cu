@@ -980,14 +980,35 @@ extern "C" int pps_check_primes_device(pps_engine* e, const pps_job_params* jp, 
   return set_err(PPS_ERR_INSUFFICIENT_RESOURCE, "hit buffer overflow persisted");
 }
 
+// The device address of a caller's host list of primes.  A page-locked
+// (pinned) buffer is read in place by the walk over the host link: each prime
+// is loaded once, 8 B per prime, a small fraction of the link's bandwidth at
+// the walk's rate.  Any other host buffer is first copied into the engine's
+// device list.
+static int host_list_on_device(pps_engine* e, const uint64_t* P, size_t np, const uint64_t** dP) {
+  *dP = nullptr;
+  if (!np) return PPS_OK;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, P) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+    *dP = (const uint64_t*)at.devicePointer;
+    return PPS_OK;
+  }
+  cudaGetLastError();  // an unregistered pointer is not an error
+  int rc;
+  if ((rc = e->P.ensure(np))) return rc;
+  CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
+  *dP = e->P.p;
+  return PPS_OK;
+}
+
 extern "C" int pps_check_primes(pps_engine* e, const pps_job_params* jp, const uint64_t* P, size_t np,
                                 pps_factor* out, size_t cap, size_t* nout, pps_job_stats* st) {
   if (!e || !jp || (!P && np)) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
   int rc;
   CU(cudaSetDevice(e->device));
-  if ((rc = e->P.ensure(np ? np : 1))) return rc;
-  if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
-  return pps_check_primes_device(e, jp, e->P.p, np, out, cap, nout, st);
+  const uint64_t* dP;
+  if ((rc = host_list_on_device(e, P, np, &dP))) return rc;
+  return pps_check_primes_device(e, jp, dP, np, out, cap, nout, st);
 }
 
 static bool hit_less(const pps_hit& x, const pps_hit& y) {
@@ -1002,14 +1023,14 @@ extern "C" int pps_check_primes_raw(pps_engine* e, const pps_job_params* jp, con
   if (np > 0xffffffffull) return set_err(PPS_ERR_INVALID_PARAM, "too many primes for one call");
   int rc;
   CU(cudaSetDevice(e->device));
-  if ((rc = e->P.ensure(np ? np : 1))) return rc;
-  if (np) CU(cudaMemcpyAsync(e->P.p, P, np * sizeof(uint64_t), cudaMemcpyHostToDevice, e->st));
+  const uint64_t* dP;
+  if ((rc = host_list_on_device(e, P, np, &dP))) return rc;
   size_t hit_cap = std::max<size_t>(1u << 20, e->hits.n);
   for (int attempt = 0; attempt < 4; ++attempt) {
     if ((rc = ensure_hit_buffers(e, hit_cap, std::max<size_t>(1u << 18, e->factors.n)))) return rc;
     e->hit_cap_limit = attempt == 0 ? debug_first_hit_cap() : 0;
     CU(cudaMemsetAsync(e->counters.p, 0, 2 * sizeof(uint32_t), e->st));
-    if (np && (rc = walk_device_list(e, jp, e->P.p, np, nullptr))) return rc;
+    if (np && (rc = walk_device_list(e, jp, dP, np, nullptr))) return rc;
     CU(cudaMemcpyAsync(e->h_pinned, e->counters.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st));
     CU(cudaStreamSynchronize(e->st));
     const uint32_t raw = ((uint32_t*)e->h_pinned)[0];

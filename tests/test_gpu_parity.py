@@ -268,3 +268,21 @@ def test_tuner_splits_small_prime_counts(pps, ref_cases):
     assert st.split >= 2, st.split
     assert lines_of(pps.factors_to_tuples(fac)) == sorted(set(case["lines"]))
     assert st.primes == case["count"]
+
+
+def test_check_primes_reads_pinned_list_in_place(pps, engine, ora):
+    """pps_check_primes on a page-locked host list (read in place by the walk)
+    and on a pageable one (copied first): the same factors, both the oracle's."""
+    torch = pytest.importorskip("torch")
+    spec = dict(pmin=10**12, pmax=10**12 + 10**7, kmin=1201, kmax=9999, nmin=2000, nmax=200000)
+    jp = pps.normalize(**spec)
+    primes = ora.sieve_range(jp.pmin, jp.pmax, jp.qmax)
+    pin = torch.empty(len(primes), dtype=torch.int64, pin_memory=True)
+    pinned = pin.numpy().view(np.uint64)
+    pinned[:] = primes
+    fac_pin, st_pin = engine.check_primes(jp, pinned)
+    fac, st = engine.check_primes(jp, primes)
+    assert st_pin.primes == st.primes == len(primes)
+    want = lines_of(ora.tuples(ora.walk_list(ora.normalize(**spec), primes)))
+    assert len(want) > 0
+    assert lines_of(pps.factors_to_tuples(fac_pin)) == lines_of(pps.factors_to_tuples(fac)) == want
