@@ -394,10 +394,10 @@ int pps_job_checkpoint(pps_server *s, uint64_t id, pps_factor *out, size_t cap, 
    until exit.  Limits: np <= PPS_NOALLOC_MAX_PRIMES per call (larger lists are
    rejected with PPS_ERR_INVALID_PARAM), and at most PPS_NOALLOC_MAX_CANDIDATES
    raw candidates per call (beyond that PPS_ERR_OVERFLOW: split the list).
-   stream: a cudaStream_t or NULL; the call returns after the work finished.
+   stream: a cudaStream_t or NULL; the call returns after the work finished
+   (it synchronises the stream, so it cannot be captured into a CUDA graph).
    The first call on a device sets the scratch up: it looks the scratch's
-   address up and copies a small-prime table into it (make that first call
-   before any stream capture).  The address is kept for the life of the
+   address up and copies a small-prime table into it.  The address is kept for the life of the
    process: cudaDeviceReset() of a set-up device is not supported (a call
    that then finds the table gone returns PPS_ERR_CUDA).  All calls on a
    device share the scratch: calls that overlap on the GPU race, so serialise
