@@ -227,6 +227,45 @@ def reference_sample(seconds_target: float = 10.0, nthreads: int | None = None,
             "n_steps_per_sec": count * steps / dt, "seconds": dt, "primes": count, "width": width}
 
 
+REF_CUDA_BIN = ROOT / "oracle" / "_ref" / "ppsieve_ref_cuda"
+
+
+def reference_gpu_sample(eng, width: int = 4 * 10**9) -> dict | None:
+    """The reference's OWN GPU program -- its main.c, sieve.c, pps/app.c and CUDA
+    kernels pps/appcu.cu, built for this GPU from the staged reference sources
+    (oracle/_ref/ppsieve_ref_cuda) -- on [4.2e13, 4.2e13 + width) of the large-n
+    Proth range, process start to exit, with its factor lines and prime
+    count/sum checked against this library's for the same range.  None where it
+    was not built here."""
+    import tempfile
+
+    import ppsgpu
+
+    if not REF_CUDA_BIN.exists():
+        return None
+    lo = LARGE_N["pmin"]
+    with tempfile.TemporaryDirectory() as td:
+        cmd = [str(REF_CUDA_BIN), f"-p{lo}", f"-P{lo + width}", "-k1201", "-K9999", "-n2000000", "-N3000000",
+               "-t1", "-q", "-fout.txt"]
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True, timeout=900)
+        dt = time.perf_counter() - t0
+        out = Path(td) / "out.txt"
+        lines = sorted(l.strip() for l in out.read_text().splitlines() if "|" in l) if out.exists() else []
+    m = FP_RE.search(r.stderr)
+    if r.returncode != 0 or not m:
+        return {"unavailable": f"exit {r.returncode}: {r.stderr.strip()[-200:]}"}
+    count, psum = int(m.group(1)), int(m.group(2), 16)
+    fac, st = eng.run_job(ppsgpu.normalize(**dict(LARGE_N, pmin=lo, pmax=lo + width)))
+    ours = sorted(ppsgpu.format_line(*t) for t in ppsgpu.factors_to_tuples(fac))
+    return {"value": count / dt, "unit": "primes/s", "kind": "reference GPU program",
+            "sample": f"p in [4.2e13, 4.2e13+{width}) = {count} primes, full n range, {dt:.2f} s wall "
+                      f"(process start to exit) with -t1; the reference's main.c/sieve.c/pps/app.c and its "
+                      f"CUDA kernels (pps/appcu.cu) built for this GPU",
+            "seconds": dt, "primes": count, "factors": len(lines),
+            "identical_to_ours": bool(lines == ours and st.primes == count and st.prime_sum == psum)}
+
+
 def baseline_sample(seconds_target: float) -> dict:
     """The CPU baseline: the reference's own CPU path where it was built here,
     with the restatement's rate beside it; the restatement alone otherwise."""
@@ -763,6 +802,7 @@ def run_gpu(args) -> None:
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                           "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
     cpu = None if args.no_cpu else baseline_sample(args.ref_seconds)
+    ref_gpu = None if args.no_cpu else reference_gpu_sample(eng)
     mixed_checked, batched = (None, None) if args.no_batched else run_mixed(eng, args.mixed_jobs)
     served, serving = (None, None) if args.no_serving else run_serving(
         window=args.serve_window, long_window=args.serve_long,
@@ -785,7 +825,8 @@ def run_gpu(args) -> None:
             "phase_ms": {"sieve": sieve_ms, "walk": walk_ms,
                          "filter": sum(s.filter_ms for s in stats)},
             "factors": sum(s.factors for s in stats),
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "reference_gpu": ref_gpu,
+            "clocks": clk.summary(),
             "batched": batched, "serving": serving, "other_workloads": others, "verify": verify}
     print(json.dumps(line), flush=True)
     eng.close()
