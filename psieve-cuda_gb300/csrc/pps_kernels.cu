@@ -13,7 +13,7 @@
 //       appended through one atomic per warp (ballot + popc ranks).
 //   k_filter
 //       output rule of pps/app.c:159-186 + pps/factor_proth.c:247-253 on the raw
-//       hits: one warp per hit, lanes split the odd primes below 32768.
+//       hits: one CTA per hit, its threads split the odd primes below 32768.
 //   k_imad_probe
 //       multiply-pipe throughput probe on the walk's multiply mix.
 #include <cuda_runtime.h>
