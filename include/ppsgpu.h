@@ -180,8 +180,10 @@ int pps_run_job(pps_engine *e, const pps_job_params *jp, pps_factor *out,
 
 /* Walk a caller-supplied list of primes held in HOST memory.  A page-locked
    (pinned) buffer, e.g. from cudaHostAlloc, is read in place by the walk over
-   the host link; any other buffer is copied to the device inside the call.
-   Same output rule and order as pps_run_job. */
+   the host link; any other buffer is copied to the device inside the call.  A
+   list that starts in page-locked memory must lie in one page-locked
+   allocation or registration (cudaHostRegister) for its whole length.  Same
+   output rule and order as pps_run_job. */
 int pps_check_primes(pps_engine *e, const pps_job_params *jp, const uint64_t *P,
                      size_t np, pps_factor *out, size_t cap, size_t *nout,
                      pps_job_stats *st);
