@@ -228,25 +228,34 @@ def reference_sample(seconds_target: float = 10.0, nthreads: int | None = None,
 
 
 REF_CUDA_BIN = ROOT / "oracle" / "_ref" / "ppsieve_ref_cuda"
+REF_CUDA_TWIN_BIN = ROOT / "oracle" / "_ref" / "tpsieve_ref_cuda"
 
 
-def reference_gpu_sample(eng, width: int = 4 * 10**9) -> dict | None:
+def _spec_args(spec: dict) -> list[str]:
+    """The reference's command-line options of a job spec (main.c / pps/app.c)."""
+    args = [f"-p{spec['pmin']}", f"-P{spec['pmax']}", f"-k{spec['kmin']}", f"-K{spec['kmax']}",
+            f"-n{spec['nmin']}", f"-N{spec['nmax']}"]
+    return args + (["-R"] if spec.get("sign") == -1 else [])
+
+
+def reference_gpu_sample(eng, width: int = 4 * 10**9, spec: dict | None = None, twin: bool = False) -> dict | None:
     """The reference's OWN GPU program -- its main.c, sieve.c, pps/app.c and CUDA
     kernels pps/appcu.cu, built for this GPU from the staged reference sources
-    (oracle/_ref/ppsieve_ref_cuda) -- on [4.2e13, 4.2e13 + width) of the large-n
-    Proth range, process start to exit, with its factor lines and prime
-    count/sum checked against this library's for the same range.  None where it
-    was not built here."""
+    (oracle/_ref/ppsieve_ref_cuda; tpsieve_ref_cuda, its twin build, for a twin
+    job) -- on `spec` (default [4.2e13, 4.2e13 + width) of the large-n Proth
+    range), process start to exit, with its factor lines and prime count/sum
+    checked against this library's for the same job.  None where it was not
+    built here."""
     import tempfile
 
     import ppsgpu
 
-    if not REF_CUDA_BIN.exists():
+    binary = REF_CUDA_TWIN_BIN if twin else REF_CUDA_BIN
+    if not binary.exists():
         return None
-    lo = LARGE_N["pmin"]
+    spec = spec or dict(LARGE_N, pmax=LARGE_N["pmin"] + width)
     with tempfile.TemporaryDirectory() as td:
-        cmd = [str(REF_CUDA_BIN), f"-p{lo}", f"-P{lo + width}", "-k1201", "-K9999", "-n2000000", "-N3000000",
-               "-t1", "-q", "-fout.txt"]
+        cmd = [str(binary), *_spec_args(spec), "-t1", "-q", "-fout.txt"]
         t0 = time.perf_counter()
         r = subprocess.run(cmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True, timeout=900)
         dt = time.perf_counter() - t0
@@ -256,12 +265,12 @@ def reference_gpu_sample(eng, width: int = 4 * 10**9) -> dict | None:
     if r.returncode != 0 or not m:
         return {"unavailable": f"exit {r.returncode}: {r.stderr.strip()[-200:]}"}
     count, psum = int(m.group(1)), int(m.group(2), 16)
-    fac, st = eng.run_job(ppsgpu.normalize(**dict(LARGE_N, pmin=lo, pmax=lo + width)))
+    fac, st = eng.run_job(ppsgpu.normalize(**dict(spec, sign=ppsgpu.PPS_SIGN_TWIN) if twin else spec))
     ours = sorted(ppsgpu.format_line(*t) for t in ppsgpu.factors_to_tuples(fac))
-    return {"value": count / dt, "unit": "primes/s", "kind": "reference GPU program",
-            "sample": f"p in [4.2e13, 4.2e13+{width}) = {count} primes, full n range, {dt:.2f} s wall "
-                      f"(process start to exit) with -t1; the reference's main.c/sieve.c/pps/app.c and its "
-                      f"CUDA kernels (pps/appcu.cu) built for this GPU",
+    return {"value": count / dt, "unit": "primes/s", "kind": "reference GPU program" + (" (twin build)" if twin else ""),
+            "sample": f"p in [{spec['pmin']}, {spec['pmax']}) = {count} primes, n in [{spec['nmin']}, "
+                      f"{spec['nmax']}), {dt:.2f} s wall (process start to exit) with -t1; the reference's "
+                      f"main.c/sieve.c/pps/app.c and its CUDA kernels (pps/appcu.cu) built for this GPU",
             "seconds": dt, "primes": count, "factors": len(lines),
             "identical_to_ours": bool(lines == ours and st.primes == count and st.prime_sum == psum)}
 
@@ -394,7 +403,70 @@ def run_other_workloads(eng) -> dict:
     out["large_n_small_range"] = {"p_range": [jp.pmin, jp.pmax], "primes": int(st.primes), **res,
                                   "speedup": res["split_1"]["seconds"] / res["tuned"]["seconds"],
                                   "identical_results": bool(np.array_equal(lists["split_1"], lists["tuned"]))}
+    out["twin_large_n_slice"] = run_twin_slice(eng)
+    out["input_file_slice"] = run_input_file_slice(eng)
     return out
+
+
+def run_twin_slice(eng) -> dict:
+    """A twin job (both k*2^n+1 and k*2^n-1 from one walk, the reference's
+    tpsieve build) on a 2^30-wide slice of the large-n range, k == 3 (mod 6) in
+    [3, 9999], timed after a warm-up; beside it the reference's own twin GPU
+    program on the same job, its lines checked against these."""
+    import ppsgpu
+
+    spec = dict(LARGE_N, pmax=LARGE_N["pmin"] + (1 << 30), kmin=3)
+    jp = ppsgpu.normalize(**dict(spec, sign=ppsgpu.PPS_SIGN_TWIN))
+    eng.run_job(jp)
+    t0 = time.perf_counter()
+    fac, st = eng.run_job(jp)
+    dt = time.perf_counter() - t0
+    return {"p_range": [jp.pmin, jp.pmax], "k": [int(jp.kmin), int(jp.kmax), int(jp.kstep)],
+            "primes": int(st.primes), "seconds": dt, "primes_per_s": st.primes / dt,
+            "n_steps_per_s": st.steps / dt, "walk_step": int(jp.step), "factors": len(fac),
+            "reference_gpu": reference_gpu_sample(eng, spec=spec, twin=True)}
+
+
+def run_input_file_slice(eng, candidates: int = 10**6) -> dict:
+    """An input sieve file (-i, NewPGen format) as the output rule: `candidates`
+    seeded (k, n) pairs of the large-n range's k and n ranges, on a 2^30-wide
+    slice, against the same slice with the small-prime filter.  Checks: every
+    line of the file run has its (k, n) in the file, and every line of the
+    other run whose (k, n) is in the file is in the file run too."""
+    import tempfile
+
+    import numpy as np
+
+    import ppsgpu
+
+    rng = np.random.default_rng(11)
+    ks = rng.integers(1201 // 2, 9999 // 2 + 1, size=candidates) * 2 + 1
+    ns = rng.integers(LARGE_N["nmin"], LARGE_N["nmax"], size=candidates)
+    order = np.lexsort((ks, ns))
+    spec = dict(LARGE_N, pmax=LARGE_N["pmin"] + (1 << 30))
+    res = {}
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "sieve.txt"
+        with open(path, "w") as f:
+            f.write("30:P:1:2:1\n")
+            f.writelines(f"{k} {n}\n" for k, n in zip(ks[order].tolist(), ns[order].tolist()))
+        # k and n bounds from the file (the reference scans a NewPGen file only
+        # when one of them is left open, pps/app.c:97, 424-434)
+        inp = ppsgpu.InputFile(path, pmin=spec["pmin"], pmax=spec["pmax"])
+        jp = ppsgpu.normalize(**inp.spec)
+        for label, use in (("small_prime_filter", None), ("input_file", inp)):
+            eng.set_input(use)
+            eng.run_job(jp)
+            t0 = time.perf_counter()
+            fac, st = eng.run_job(jp)
+            dt = time.perf_counter() - t0
+            res[label] = {"seconds": dt, "primes_per_s": st.primes / dt, "factors": len(fac),
+                          "filter_ms": st.filter_ms, "lines": set(ppsgpu.factors_to_tuples(fac))}
+        eng.set_input(None)
+    in_file = set(zip(ks.tolist(), ns.tolist()))
+    got, other = res["input_file"].pop("lines"), res["small_prime_filter"].pop("lines")
+    ok = all((k, n) in in_file for _, k, n, _ in got) and all(t in got for t in other if (t[1], t[2]) in in_file)
+    return {"p_range": [jp.pmin, jp.pmax], "candidates": candidates, **res, "consistent_with_file": bool(ok)}
 
 
 def _serve_rate(srv, pool, nxt: int, rng, rate: float, window: float, max_jobs: int, served: list,
