@@ -257,7 +257,11 @@ def reference_gpu_sample(eng, width: int = 4 * 10**9, spec: dict | None = None, 
     with tempfile.TemporaryDirectory() as td:
         cmd = [str(binary), *_spec_args(spec), "-t1", "-q", "-fout.txt"]
         t0 = time.perf_counter()
-        r = subprocess.run(cmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True, timeout=900)
+        try:
+            r = subprocess.run(cmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True,
+                               timeout=900)
+        except (subprocess.TimeoutExpired, OSError) as ex:
+            return {"unavailable": f"{binary.name}: {type(ex).__name__}"}
         dt = time.perf_counter() - t0
         out = Path(td) / "out.txt"
         lines = sorted(l.strip() for l in out.read_text().splitlines() if "|" in l) if out.exists() else []
