@@ -1240,10 +1240,13 @@ int batch_wave(pps_engine* e, const BatchPiece* pieces, size_t n, std::vector<pp
   };
 
   if (!b->tuned_work) {
-    // time each (work per chunk, unroll, one or two primes per lane) on the
-    // first chunks of this wave, the same number of walk steps for every candidate
+    // time each (work per chunk, unroll) on the first chunks of this wave, the
+    // same number of walk steps for every candidate.  The kernels take two
+    // primes per lane: on the 512-job mix, each kind of job alone walked as
+    // fast or faster with them than with one prime per lane at the same unroll
+    // (pps_engine_set_batch_walk still forces one prime per lane).
     const int works[] = {256, 1024, 4096};
-    const int unrolls[] = {8, 16, 8 | WALK_TWO, 16 | WALK_TWO};
+    const int unrolls[] = {8 | WALK_TWO, 16 | WALK_TWO};
     float best = 1e30f;
     for (int w : works)
       for (int u : unrolls) {
