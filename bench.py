@@ -934,6 +934,8 @@ def run_profile_batched(args) -> None:
     eng = ppsgpu.Engine(0)
     if args.wave_segments:
         eng.set_wave_segments(args.wave_segments)  # smaller waves: less device memory (captures)
+    if args.batch_walk:
+        eng.set_batch_walk(*args.batch_walk)  # a fixed walk kernel (unroll, primes per lane)
     jobs, _ = ppsgpu.mixed_jobs(seed=1, count=args.mixed_jobs)
     eng.run_batch(jobs[:64])
     t0 = time.perf_counter()
@@ -969,6 +971,8 @@ def main() -> None:
     ap.add_argument("--profile-batched", action="store_true")
     ap.add_argument("--wave-segments", type=int, default=0,
                     help="--profile-batched: segments per wave (0: the maximum, 16384)")
+    ap.add_argument("--batch-walk", type=int, nargs=2, metavar=("UNROLL", "PRIMES_PER_LANE"),
+                    help="--profile-batched: force the batched walk kernel (8 or 16, 1 or 2)")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
