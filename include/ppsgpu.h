@@ -281,7 +281,8 @@ int pps_engine_set_wave_segments(pps_engine *e, uint32_t segments);
 
 /* Force the batched form's walk kernel: unroll 8 or 16 steps per block, 1 or
    2 primes per lane for the 32-bit-step jobs (2: the 64-register kernel); 0, 0
-   for the choice the first wave's timing makes (reported in pps_batch_stats). */
+   for the choice the first wave's timing makes among the two-primes-per-lane
+   kernels (reported in pps_batch_stats). */
 int pps_engine_set_batch_walk(pps_engine *e, int unroll, int primes_per_lane);
 
 /* Per-job prime count and wrapping prime sum of the last pps_run_batch. */
