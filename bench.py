@@ -14,9 +14,10 @@ larger than the 129 MB L2, so no flush is needed between steps).
 value  = primes fully walked per second (whole job, all ranks).
 e2e    = the same metric through the drop-in C-ABI call with HOST buffers:
          pps_check_primes() given the slice's primes in pinned host memory
-         (H2D copy inside the timed region) and returning the factor list to the
-         host (D2H inside the timed region) -- what the reference's check_ns /
-         get_factors_found boundary carries.
+         (read by the walk in place over the host link, inside the timed
+         region) and returning the factor list to the host (D2H inside the
+         timed region) -- what the reference's check_ns / get_factors_found
+         boundary carries.
 roofline: the walk kernel is bound by the 32-bit integer multiply pipe; its
          algorithmic work is 3 multiplies per walk step (one 32 n-values advance
          of one prime); the peak is the multiply-pipe throughput measured in this
@@ -29,6 +30,13 @@ verify : the checker leg, after every timed leg and not timed: the large-n
          line by the oracle on the host cores, and the prime count and sum of
          every full-range slice (and of 16 seeded mixed jobs) are compared with
          the oracle's sieve.
+reference_gpu: the reference's own GPU program (its main.c, sieve.c, pps/app.c
+         and CUDA kernels built for this GPU from the staged reference sources)
+         on a 4e9-wide slice of the same range, process start to exit, its
+         factor lines and prime count/sum compared with this library's.
+other_workloads: the small Proth range in full, a 62-bit Riesel slice, a
+         2e6-wide large-n range (threads per prime), a twin slice beside the
+         reference's own twin GPU program, and a slice with an input sieve file.
 --impl reference: the reference's own CPU path (main.c, sieve.c, pps/app.c,
          pps/factor_proth.c compiled on this host from the staged reference
          sources; every prime re-walked by pps/app.c's test_one_p) on all host
