@@ -50,11 +50,12 @@ extern "C" {
    reference's twin build (tpsieve, -DSEARCH_TWIN: pps/app.c:1071-1107,
    pps/appcu.cu:177-180, 741-767) reports them; k == 3 (mod 6) unless -M/-s
    say otherwise.  Each factor carries its own c.  pps_run_job, pps_run_batch
-   and the serving loop run twin jobs on the batched walk; pps_check_primes*
-   on the one-job twin kernels (which need s = 32, or p <= 2^(32+s):
-   PPS_ERR_NOT_IMPLEMENTED otherwise; raw candidates of a twin job carry their
-   side in idx bit 31).  The appcu.h layer and pps_check_primes_noalloc take
-   one side only. */
+   and the serving loop run twin jobs on the batched walk; pps_check_primes*,
+   and pps_run_job with an input file, on the one-job twin kernels (which need
+   s = 32, or p <= 2^(32+s): PPS_ERR_NOT_IMPLEMENTED otherwise; raw candidates
+   of a twin job carry their side in idx bit 31).  An input file for a twin job
+   is in the twin build's formats (pps_input_read).  The appcu.h layer and
+   pps_check_primes_noalloc take one side only. */
 #define PPS_SIGN_TWIN 2
 
 /* A job as the user states it; zero means "not given" exactly as in the
@@ -228,7 +229,15 @@ uint64_t pps_engine_launches(const pps_engine *e);
    (nmax one past the largest n).  When all four are given the file is read as
    ABCD without a scan (pps/app.c:97), so a NewPGen file is refused.  Errors:
    PPS_ERR_FOPEN, PPS_ERR_SCANF.  Entries the reference would write outside its
-   bitmap (an ABCD k below kmin or past kmax; n past nmax) are ignored. */
+   bitmap (an ABCD k below kmin or past kmax; n past nmax) are ignored.
+
+   For a twin job (spec->sign == PPS_SIGN_TWIN) the file is in the formats of
+   the reference's twin build (pps/app.c:208-216): NewPGen "p0:T:x:2:3" then
+   "k n" lines, or ABCD "ABCD (6*$a+3)*2^n+1 & (6*$a+3)*2^n-1 [a0]" per n then
+   deltas of the k index a (k = kstep a + koffset; the extents reported are k
+   values).  A factor of either side is reported iff its (k, n) is in the
+   file.  One-side formats are refused for a twin job and twin formats for a
+   one-side job, as each reference build does. */
 typedef struct pps_input pps_input;
 
 typedef struct {

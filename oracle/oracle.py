@@ -236,6 +236,7 @@ def parse_line(line: str) -> tuple[int, int, int, int]:
 # ---------------------------------------------------------------- input files
 
 ERR_SCANF = -140  # pps/app.h:69
+TWIN = 2  # sign of a twin job (PPO_TWIN)
 
 
 class InputFile:
@@ -252,13 +253,63 @@ class InputFile:
         self.n0, self.n1 = min(ns), max(ns) + 1
 
 
-def read_input(path, detect: bool = True) -> InputFile:
+def read_twin_input(path, detect: bool = True) -> InputFile:
+    """The twin build's formats (pps/app.c:208-216 headers, 242-309 scan,
+    349-517 read with SEARCH_TWIN): NewPGen "p0:T:x:2:3" then "k n" lines, or
+    ABCD "ABCD (6*$a+3)*2^n+1 & (6*$a+3)*2^n-1 [a0]" per n with a deltas, a
+    being the k index (k = kstep a + koffset).  ABCD records hold (a, n) and
+    format "abcd_twin"; the scan's k extents are indices too (converted in
+    input_spec, pps/app.c:325-331)."""
+    import re
+
+    text = open(path).read().splitlines()
+    hdr = r"\s*ABCD \(6\*\$a\+3\)\*2\^(\d+)\+1 & \(6\*\$a\+3\)\*2\^(\d+)-1 \[(\d+)\]"
+    m = re.match(hdr, text[0]) if text else None
+    if m and m.group(1) == m.group(2):
+        recs, n, a = [], int(m.group(1)), int(m.group(3))
+        recs.append((a, n))
+        for line in text[1:]:
+            h = re.match(hdr, line)
+            if h:
+                if h.group(1) != h.group(2):
+                    break
+                n, a = int(h.group(1)), int(h.group(3))
+                recs.append((a, n))
+                continue
+            d = re.match(r"(\d+)", line)
+            if not d:
+                if line.strip():
+                    break
+                continue  # blank line
+            a += int(d.group(1))
+            recs.append((a, n))
+        return InputFile("abcd_twin", TWIN, recs)
+    if not detect:
+        raise OracleError(ERR_SCANF)
+    m = re.match(r"\s*(\d+):T:.:2:(.)", text[0]) if text else None
+    if not m or m.group(2) != "3":
+        raise OracleError(ERR_SCANF)
+    recs = []
+    for line in text[1:]:
+        f = line.split()
+        if len(f) < 2:
+            break
+        recs.append((int(f[0]), int(f[1])))
+    if not recs:
+        raise OracleError(ERR_SCANF)  # "Invalid line 2"
+    return InputFile("newpgen", TWIN, recs)
+
+
+def read_input(path, detect: bool = True, twin: bool = False) -> InputFile:
     """Format detection and parsing (pps/app.c:208-231 headers, 242-309 scan,
     349-517 read).  The reference detects the format only while scanning (when
     one of kmin, kmax, nmin, nmax is not given); otherwise it reads the file as
-    ABCD (pps/app.c:97), and a NewPGen file is an invalid header."""
+    ABCD (pps/app.c:97), and a NewPGen file is an invalid header.  twin: the
+    twin build's formats (read_twin_input)."""
     import re
 
+    if twin:
+        return read_twin_input(path, detect)
     text = open(path).read().splitlines()
     m = re.match(r"ABCD (\d+)\*2\^\$a([+-])1 \[(\d+)\]", text[0]) if text else None
     if not m and not detect:
@@ -302,9 +353,14 @@ def input_spec(inp: InputFile, spec: dict) -> dict:
     if all(spec.get(f) for f in ("kmin", "kmax", "nmin", "nmax")):
         return spec
     spec["sign"] = inp.sign
-    spec["kmin"] = max(spec.get("kmin") or 0, inp.k0)
-    if not spec.get("kmax") or spec["kmax"] > inp.k1:
-        spec["kmax"] = inp.k1
+    k0, k1 = inp.k0, inp.k1
+    if inp.format == "abcd_twin":  # indices to k (pps/app.c:325-331)
+        kstep = spec.get("kstep") or 6
+        koffset = spec.get("koffset") or 3
+        k0, k1 = kstep * k0 + koffset, kstep * k1 + koffset
+    spec["kmin"] = max(spec.get("kmin") or 0, k0)
+    if not spec.get("kmax") or spec["kmax"] > k1:
+        spec["kmax"] = k1
     spec["nmin"] = max(spec.get("nmin") or 0, inp.n0)
     if not spec.get("nmax") or spec["nmax"] > inp.n1:
         spec["nmax"] = inp.n1
@@ -327,6 +383,12 @@ def input_keys(inp: InputFile, params: Params) -> np.ndarray:
             if not (params.kmin <= k <= params.kmax):
                 continue
             bit = k // kstep - b0
+        elif inp.format == "abcd_twin":  # k is the index a (pps/app.c:451, 484)
+            if k < b0:
+                continue
+            bit = k - b0
+            if bit >= width:
+                continue
         else:
             if k < params.kmin:
                 continue

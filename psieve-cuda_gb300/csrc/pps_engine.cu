@@ -899,7 +899,16 @@ extern "C" int pps_run_job(pps_engine* e, const pps_job_params* jp, pps_factor* 
                            size_t* nout, pps_job_stats* st) {
   if (!e || !jp) return set_err(PPS_ERR_INVALID_PARAM, "null argument");
   if (jp->step < 1 || jp->step > 32 || jp->pmin <= (1ull << 32)) return set_err(PPS_ERR_INVALID_PARAM, "job not normalized");
-  if (jp->sign == PPS_SIGN_TWIN) return run_twin_job(e, jp, out, cap, nout, st);
+  if (jp->sign == PPS_SIGN_TWIN) {
+    // twin jobs run on the batched walk, except with an input file: its rule
+    // applies on the one-job path, whose twin kernels need 32-bit steps or
+    // p <= 2^(32+s)
+    if (!e->input) return run_twin_job(e, jp, out, cap, nout, st);
+    bool exact = false;
+    for (int v = 0; v < PPS_NUM_VARIANTS && !exact; ++v) exact = variant_ok(jp, v) != 0;
+    if (!exact)
+      return set_err(PPS_ERR_NOT_IMPLEMENTED, "a twin job with an input file needs 32-bit steps or p <= 2^(32+s)");
+  }
   CU(cudaSetDevice(e->device));
   size_t hit_cap = 1u << 20, fac_cap = 1u << 18;
   for (int attempt = 0; attempt < 4; ++attempt) {

@@ -3,7 +3,8 @@
 // Host code only.  Restates the reference's file handling:
 //   scan_input_file   pps/app.c:190-347  format detection, extents, side
 //   read_newpgen_file pps/app.c:349-401  "k n" lines into the bitmap
-//   read_abcd_file    pps/app.c:403-517  per-k blocks of n deltas
+//   read_abcd_file    pps/app.c:403-517  per-k blocks of n deltas (the twin
+//                     build: per-n blocks of k-index deltas)
 //   test_factor       pps/app.c:180-183  the bitmap as the output rule
 // The reference's bitmap (one bit per (n - nmin, (k - kmin) / kstep)) becomes a
 // sorted table of those bit numbers, which the device filter searches.
@@ -21,7 +22,8 @@
 
 struct pps_input {
   int32_t format = 0;  // 1 NewPGen, 2 ABCD
-  int32_t sign = 1;
+  int32_t sign = 1;    // PPS_SIGN_TWIN for the twin build's formats
+  bool k_index = false;  // twin ABCD: records hold the k index a (k = kstep a + koffset)
   std::vector<std::pair<uint64_t, uint32_t>> recs;  // (k, n) in file order
   uint64_t k0 = 0, k1 = 0;
   uint32_t n0 = 0, n1 = 0;
@@ -33,6 +35,13 @@ constexpr int32_t FORMAT_NEWPGEN = 1, FORMAT_ABCD = 2;  // pps/app.c:81-82
 
 bool abcd_header(const char* line, uint64_t* k, char* ch, uint32_t* n) {
   return sscanf(line, " ABCD %" SCNu64 "*2^$a%c1 [%u]", k, ch, n) == 3;
+}
+
+// The twin build's ABCD header (pps/app.c:212-213, 429-431): one n, both sides,
+// the first k index a.
+bool twin_abcd_header(const char* line, uint32_t* n, uint64_t* a) {
+  uint32_t m = 0;
+  return sscanf(line, " ABCD (6*$a+3)*2^%u+1 & (6*$a+3)*2^%u-1 [%" SCNu64 "]", &m, n, a) == 3 && m == *n;
 }
 
 }  // namespace
@@ -69,7 +78,42 @@ extern "C" int pps_input_read(const char* path, pps_job_spec* spec, pps_input** 
   uint64_t k = 0;
   uint32_t n = 0;
   char ch = 0;
-  if (!lines.empty() && abcd_header(lines[0].c_str(), &k, &ch, &n)) {
+  if (spec->sign == PPS_SIGN_TWIN) {
+    // the twin build's formats (pps/app.c:208-216): ABCD per n with k-index
+    // deltas, or NewPGen ":T:" -- the latter only while scanning
+    in->sign = PPS_SIGN_TWIN;
+    if (!lines.empty() && twin_abcd_header(lines[0].c_str(), &n, &k)) {
+      in->format = FORMAT_ABCD;
+      in->k_index = true;
+      in->recs.emplace_back(k, n);
+      for (size_t i = 1; i < lines.size(); ++i) {
+        const char* s = lines[i].c_str();
+        if (s[0] >= '0' && s[0] <= '9') {  // a k-index delta (pps/app.c:258-262, 474-477)
+          k += strtoull(s, nullptr, 10);
+          in->recs.emplace_back(k, n);
+        } else if (twin_abcd_header(s, &n, &k)) {
+          in->recs.emplace_back(k, n);
+        } else if (s[strspn(s, " \t\r")] != '\0') {
+          break;
+        }
+      }
+    } else if (scan) {
+      uint64_t p0 = 0;
+      if (lines.empty() || sscanf(lines[0].c_str(), " %" SCNu64 ":T:%*c:2:%c", &p0, &ch) != 2 || ch != '3')
+        return fail("Invalid header in input file");
+      in->format = FORMAT_NEWPGEN;
+      for (size_t i = 1; i < lines.size(); ++i) {
+        if (sscanf(lines[i].c_str(), " %" SCNu64 " %u", &k, &n) != 2) {
+          if (lines[i].find_first_not_of(" \t\r") == std::string::npos) continue;
+          break;
+        }
+        in->recs.emplace_back(k, n);
+      }
+      if (in->recs.empty()) return fail("Invalid line 2 in input file");
+    } else {
+      return fail("Invalid header in input file");  // read as ABCD (pps/app.c:97)
+    }
+  } else if (!lines.empty() && abcd_header(lines[0].c_str(), &k, &ch, &n)) {
     in->format = FORMAT_ABCD;
     in->sign = ch == '+' ? 1 : -1;
     in->recs.emplace_back(k, n);
@@ -112,6 +156,11 @@ extern "C" int pps_input_read(const char* path, pps_job_spec* spec, pps_input** 
     in->n1 = std::max(in->n1, r.second);
   }
   in->n1++;  // pps/app.c:319
+  if (in->k_index) {  // the indices as k (pps/app.c:325-331)
+    const uint64_t kstep = spec->kstep ? spec->kstep : 6, koffset = spec->koffset ? spec->koffset : 3;
+    in->k0 = kstep * in->k0 + koffset;
+    in->k1 = kstep * in->k1 + koffset;
+  }
   if (scan) {  // pps/app.c:335-346, and the side from the header (pps/app.c:216, 225)
     spec->sign = in->sign;
     if (spec->kmin < in->k0) spec->kmin = in->k0;
@@ -191,6 +240,10 @@ int input_keys_for_job(const pps_input* in, const pps_job_params* jp, std::vecto
       if (k % kstep != koffset) return set_err(PPS_ERR_SCANF, "Invalid line in input file: k=%" PRIu64, k);
       if (k < jp->kmin || k > jp->kmax) continue;
       bit = k / kstep - b0;  // pps/app.c:392
+    } else if (in->k_index) {
+      if (k < b0) continue;  // k is the twin build's index a (pps/app.c:451, 484)
+      bit = k - b0;
+      if (bit >= w) continue;
     } else {
       if (k < jp->kmin) continue;  // the reference writes before its bitmap here
       bit = (k - jp->kmin) / kstep;  // pps/app.c:438-441

@@ -155,15 +155,10 @@ void app_init(void)
 #endif
   spec.kstep = kstep;
   spec.koffset = koffset;
-#ifdef PPS_TWIN
-  if (input_filename != NULL) {
-    bmsg("The twin build's input formats are not supported\n");
-    bexit(-150);
-  }
-#endif
   if (input_filename != NULL) {
     /* pps/app.c:661-663 and 726-738: the file fills the bounds the command
-       line left open, and becomes the output rule */
+       line left open, and becomes the output rule (the twin build reads the
+       twin formats, pps/app.c:208-216) */
     const int rc = pps_input_read(input_filename, &spec, &input_set);
     if (rc == PPS_ERR_FOPEN) {
       perror(input_filename);
@@ -173,7 +168,9 @@ void app_init(void)
       fprintf(stderr, "%s%s\n", bmprefix(), pps_last_error());
       bexit(ERR_SCANF);
     }
-    search_proth = spec.sign;
+#ifndef PPS_TWIN
+    search_proth = spec.sign;  /* the twin build's files are twin (both sides) */
+#endif
   }
   if (pps_normalize(&spec, &job) != PPS_OK) {
     char msg[600];

@@ -9,6 +9,7 @@ compiled into oracle/_ref/ (the "files" step also reads the reference's shipped
 golden lists, from the checkout named by PPS_REFERENCE):
   ppsieve_ref        the reference's main.c/sieve.c/pps/app.c/pps/factor_proth.c with
                      the CPU stand-in for pps/appcu.h (every subsection flagged);
+  tpsieve_ref        its twin build (-DSEARCH_TWIN; steps "twin" and "twin_input");
   ppsieve_ref_fixed  the same with the 64-bit fix at pps/app.c:1087 (used where
                      nstep >= 48, where the unfixed re-walk misses factors).
 Each case records the command line, the sorted factor lines and the reference's
@@ -201,6 +202,84 @@ def write_abcd(path: Path, pairs, c: int) -> None:
     path.write_text("\n".join(out) + "\n")
 
 
+def _twin_survivors(kmin: int, kmax: int, nmin: int, nmax: int) -> list[tuple[int, int]]:
+    """(k, n) with k == 3 (mod 6), nmin <= n <= nmax, both k*2^n+1 and k*2^n-1
+    free of the primes below 30: a stand-in for a twin sieve's output."""
+    out = []
+    for k in range(kmin + (3 - kmin) % 6, kmax + 1, 6):
+        for n in range(nmin, nmax + 1):
+            if all((k * pow(2, n, q) + 1) % q and (k * pow(2, n, q) - 1) % q for q in SMALL_Q):
+                out.append((k, n))
+    return out
+
+
+def write_twin_newpgen(path: Path, pairs) -> None:
+    """The twin build's NewPGen format (pps/app.c:214-215, 360-365): "p0:T:x:2:3"
+    then "k n" lines."""
+    lines = ["30:T:1:2:3"] + [f"{k} {n}" for k, n in sorted(pairs)]
+    path.write_text("\n".join(lines) + "\n")
+
+
+def write_twin_abcd(path: Path, pairs) -> None:
+    """The twin build's ABCD format (pps/app.c:212-213, 429-500): per n a header
+    "ABCD (6*$a+3)*2^n+1 & (6*$a+3)*2^n-1 [a0]" with k = 6a + 3, then one a
+    delta per line."""
+    by_n: dict[int, list[int]] = {}
+    for k, n in sorted(pairs, key=lambda t: (t[1], t[0])):
+        by_n.setdefault(n, []).append((k - 3) // 6)
+    out = []
+    for n, a in sorted(by_n.items()):
+        out.append(f"ABCD (6*$a+3)*2^{n}+1 & (6*$a+3)*2^{n}-1 [{a[0]}] // sieved to 30")
+        out += [str(y - x) for x, y in zip(a, a[1:])]
+    path.write_text("\n".join(out) + "\n")
+
+
+def make_twin_input_cases() -> None:
+    """Synthetic twin sieve files in both of the twin build's formats, and the
+    reference's twin build's own output when given each with -i."""
+    INPUTS.mkdir(exist_ok=True)
+    pairs = _twin_survivors(3, 99, 1000, 2999)
+    write_twin_newpgen(INPUTS / "twin_newpgen.txt", pairs)
+    write_twin_abcd(INPUTS / "twin_abcd.txt", pairs)
+    print("twin input pairs:", len(pairs), flush=True)
+    lo = 5 * 10**10
+    rng = [f"-p{lo}", f"-P{lo + 10**9}"]
+    cases = [
+        ("twin_in_newpgen", "twin_newpgen.txt", rng),
+        ("twin_in_abcd", "twin_abcd.txt", rng),
+        # a partial override: kmax given, the rest from the file
+        ("twin_in_abcd_kmax", "twin_abcd.txt", [*rng, "-K51"]),
+        # all of k/n given: the file is read as ABCD without a scan (pps/app.c:97);
+        # the ranges cover the file's, so the reference's bitmap holds every entry
+        ("twin_in_abcd_given", "twin_abcd.txt", [*rng, "-k3", "-K99", "-n1000", "-N3000"]),
+        # and a NewPGen file is then an invalid header (ERR_SCANF)
+        ("twin_in_newpgen_given", "twin_newpgen.txt", [*rng, "-k3", "-K99", "-n1000", "-N3000"]),
+    ]
+    binary = REF_DIR / "tpsieve_ref"
+
+    def one(case):
+        name, f, args = case
+        with tempfile.TemporaryDirectory() as td:
+            cmd = [str(binary), *args, f"-i{INPUTS / f}", "-t2", "-m8192", "-c1000000", "-r1000000", "-q",
+                   "-fout.txt"]
+            r = subprocess.run(cmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True,
+                               timeout=1200)
+            out = Path(td, "out.txt")
+            lines = [l.strip() for l in out.read_text().splitlines() if "|" in l] if out.exists() else []
+        m = FP_RE.search(r.stderr)
+        res = {"args": args, "input": f, "binary": binary.name, "rc": r.returncode, "lines": sorted(lines),
+               "unique": len(set(lines)), "total": len(lines)}
+        if m:
+            res["count"] = int(m.group(1))
+            res["sum"] = "0x" + m.group(2)
+        print(f"{name}: {len(lines)} lines rc={r.returncode}", flush=True)
+        return name, res
+
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        out = dict(ex.map(one, cases))
+    (HERE / "twin_input_cases.json").write_text(json.dumps(out, indent=1, sort_keys=True))
+
+
 def make_input_cases() -> None:
     """Synthetic sieve files in both formats and both signs, and the reference's
     own output when given each with -i (bitmap output rule, pps/app.c:180-183)."""
@@ -347,6 +426,8 @@ def main() -> None:
         (HERE / "twin_cases.json").write_text(json.dumps(out, indent=1, sort_keys=True))
     if "input" in which:
         make_input_cases()
+    if "twin_input" in which:
+        make_twin_input_cases()
     if "kat" in which:
         kats = planted_kat49()
         out = []

@@ -128,3 +128,30 @@ def test_twin_plugin_factor_file(twin_driver, tmp_path, ora, name):
     lines = sorted(l for l in ff.read_text().splitlines() if "|" in l) if ff.exists() else []
     assert lines == case["lines"]
     assert f"count={case['count']}," in r.stdout
+
+
+@pytest.mark.parametrize("name", ["twin_in_newpgen", "twin_in_abcd", "twin_in_abcd_given"])
+def test_twin_plugin_input_file(twin_driver, tmp_path, ora, name):
+    """-i with the twin build: a file in the twin build's formats is the output
+    rule for both sides; the factor file equals the reference's own twin build
+    run with the same file (tests/golden/twin_input_cases.json)."""
+    import json
+
+    import math
+
+    case = json.loads((GOLDEN / "twin_input_cases.json").read_text())[name]
+    spec = args_to_spec(case["args"])
+    # the first 4e8 of the fixture's p range (its lines there), to keep the prime file small
+    lo, hi = spec["pmin"], spec["pmin"] + 4 * 10**8
+    primes = ora.sieve_range(lo | 1, hi, math.isqrt(hi))
+    pf = tmp_path / "primes.bin"
+    primes.astype("<u8").tofile(pf)
+    ff = tmp_path / "factors.txt"
+    args = [a for a in case["args"] if not a.startswith(("-p", "-P"))]
+    r = subprocess.run([str(twin_driver), str(pf), f"-p{lo}", f"-P{hi}", *args,
+                        f"-i{GOLDEN / 'inputs' / case['input']}", f"-f{ff}", "-m1"],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr
+    lines = sorted(l for l in ff.read_text().splitlines() if "|" in l) if ff.exists() else []
+    want = sorted(l for l in case["lines"] if int(l.split("|")[0]) < hi)
+    assert lines == want and {l[-2:] for l in want} == {"+1", "-1"}

@@ -52,3 +52,36 @@ def test_input_reader_errors(pps, tmp_path):
     with pytest.raises(pps.PPSError) as ei:
         pps.InputFile(one, pmin=10**12, pmax=10**12 + 10**6)
     assert ei.value.code == pps.PPS_ERR_SCANF
+
+
+def test_twin_input_reader_matches_oracle(pps, ora):
+    """The twin build's formats, read for a twin job (sign PPS_SIGN_TWIN)."""
+    cases = json.loads((GOLDEN / "twin_input_cases.json").read_text())
+    for name, case in sorted(cases.items()):
+        spec = dict(args_to_spec(case["args"]), sign=pps.PPS_SIGN_TWIN)
+        path = GOLDEN / "inputs" / case["input"]
+        given = all(spec[f] for f in ("kmin", "kmax", "nmin", "nmax"))
+        if case["rc"] != 0:
+            with pytest.raises(pps.PPSError) as ei:
+                pps.InputFile(path, **spec)
+            assert ei.value.code == pps.PPS_ERR_SCANF
+            with pytest.raises(ora.OracleError):
+                ora.read_input(path, detect=not given, twin=True)
+            continue
+        inp = pps.InputFile(path, **spec)
+        oi = ora.read_input(path, detect=not given, twin=True)
+        info = inp.info()
+        k0, k1 = (6 * oi.k0 + 3, 6 * oi.k1 + 3) if oi.format == "abcd_twin" else (oi.k0, oi.k1)
+        assert info.records == len(oi.records), name
+        assert (info.k0, info.k1, info.n0, info.n1) == (k0, k1, oi.n0, oi.n1), name
+        assert {"newpgen": 1, "abcd_twin": 2}[oi.format] == info.format, name
+        assert info.sign == oi.sign == pps.PPS_SIGN_TWIN, name
+        ospec = ora.input_spec(oi, spec)
+        for f in ("kmin", "kmax", "nmin", "nmax", "sign"):
+            assert inp.spec[f] == ospec[f], (name, f)
+    # a one-side file for a twin job, and a twin file for a one-side job, are refused
+    with pytest.raises(pps.PPSError):
+        pps.InputFile(GOLDEN / "inputs" / "newpgen_proth.txt", pmin=5 * 10**10, pmax=6 * 10**10,
+                      sign=pps.PPS_SIGN_TWIN)
+    with pytest.raises(pps.PPSError):
+        pps.InputFile(GOLDEN / "inputs" / "twin_newpgen.txt", pmin=5 * 10**10, pmax=6 * 10**10)
