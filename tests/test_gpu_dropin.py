@@ -3,6 +3,8 @@
   ppsieve_gpu     main.c + sieve.c + putil.c + clock.c with the GPU plugin
                   (libppsgpu_app.so, include/pps_app.h) in place of pps/app.c +
                   pps/appcu.cu + pps/factor_proth.c;
+  tpsieve_gpu     the same with the plugin's twin build (libppsgpu_app_twin.so),
+                  the reference's tpsieve;
   ppsieve_dropin  main.c + sieve.c + the reference's unmodified pps/app.c and
                   pps/factor_proth.c, with the GPU library's pps/appcu.h ABI
                   (libppsgpu_appcu.so, include/appcu_compat.h) in place of
@@ -71,3 +73,28 @@ def test_reference_main_cases(built, binary, name, tmp_path, ref_cases):
     assert lines == case["lines"], name
     assert fp is not None, err[-400:]
     assert int(fp.group(1)) == case["count"] and int(fp.group(2), 16) == int(case["sum"], 16)
+
+
+def test_twin_dropin_matches_reference_twin_build(built, tmp_path):
+    """tpsieve_gpu: the reference's main.c and sieve.c with the plugin's twin
+    build, against the reference's own twin build (tests/golden/twin_cases.json)."""
+    import json
+
+    case = json.loads((GOLDEN / "twin_cases.json").read_text())["twin_small"]
+    lines, fp, err = _run(_binary("tpsieve_gpu"), [*case["args"], "-q"], tmp_path)
+    assert lines == case["lines"]
+    assert fp is not None, err[-400:]
+    assert int(fp.group(1)) == case["count"] and int(fp.group(2), 16) == int(case["sum"], 16)
+
+
+@pytest.mark.parametrize("name", ["twin_in_abcd", "twin_in_newpgen"])
+def test_twin_dropin_input_file(built, tmp_path, name):
+    """tpsieve_gpu with -i and a file in the twin build's formats, against the
+    reference's twin build run with the same file."""
+    import json
+
+    case = json.loads((GOLDEN / "twin_input_cases.json").read_text())[name]
+    lines, fp, err = _run(_binary("tpsieve_gpu"), [*case["args"], f"-i{GOLDEN / 'inputs' / case['input']}",
+                                                   "-q"], tmp_path)
+    assert lines == case["lines"]
+    assert fp is not None and int(fp.group(1)) == case["count"], err[-400:]
