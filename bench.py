@@ -246,7 +246,11 @@ def _spec_args(spec: dict) -> list[str]:
     return args + (["-R"] if spec.get("sign") == -1 else [])
 
 
-def reference_gpu_sample(eng, width: int = 4 * 10**9, spec: dict | None = None, twin: bool = False) -> dict | None:
+DROPIN_BIN = ROOT / "oracle" / "_ref" / "ppsieve_gpu"
+
+
+def reference_gpu_sample(eng, width: int = 4 * 10**9, spec: dict | None = None, twin: bool = False,
+                         binary: Path | None = None, threads: int = 1) -> dict | None:
     """The reference's OWN GPU program -- its main.c, sieve.c, pps/app.c and CUDA
     kernels pps/appcu.cu, built for this GPU from the staged reference sources
     (oracle/_ref/ppsieve_ref_cuda; tpsieve_ref_cuda, its twin build, for a twin
@@ -258,12 +262,12 @@ def reference_gpu_sample(eng, width: int = 4 * 10**9, spec: dict | None = None, 
 
     import ppsgpu
 
-    binary = REF_CUDA_TWIN_BIN if twin else REF_CUDA_BIN
+    binary = binary or (REF_CUDA_TWIN_BIN if twin else REF_CUDA_BIN)
     if not binary.exists():
         return None
     spec = spec or dict(LARGE_N, pmax=LARGE_N["pmin"] + width)
     with tempfile.TemporaryDirectory() as td:
-        cmd = [str(binary), *_spec_args(spec), "-t1", "-q", "-fout.txt"]
+        cmd = [str(binary), *_spec_args(spec), f"-t{threads}", "-q", "-fout.txt"]
         t0 = time.perf_counter()
         try:
             r = subprocess.run(cmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True,
@@ -279,10 +283,14 @@ def reference_gpu_sample(eng, width: int = 4 * 10**9, spec: dict | None = None, 
     count, psum = int(m.group(1)), int(m.group(2), 16)
     fac, st = eng.run_job(ppsgpu.normalize(**dict(spec, sign=ppsgpu.PPS_SIGN_TWIN) if twin else spec))
     ours = sorted(ppsgpu.format_line(*t) for t in ppsgpu.factors_to_tuples(fac))
-    return {"value": count / dt, "unit": "primes/s", "kind": "reference GPU program" + (" (twin build)" if twin else ""),
+    what = ("the reference's main.c/sieve.c with this library's plugin (libppsgpu_app.so) in place of "
+            "pps/app.c + pps/appcu.cu" if binary == DROPIN_BIN else
+            "the reference's main.c/sieve.c/pps/app.c and its CUDA kernels (pps/appcu.cu) built for this GPU")
+    kind = ("drop-in: the reference's main.c and sieve.c with this library's plugin" if binary == DROPIN_BIN
+            else "reference GPU program" + (" (twin build)" if twin else ""))
+    return {"value": count / dt, "unit": "primes/s", "kind": kind,
             "sample": f"p in [{spec['pmin']}, {spec['pmax']}) = {count} primes, n in [{spec['nmin']}, "
-                      f"{spec['nmax']}), {dt:.2f} s wall (process start to exit) with -t1; the reference's "
-                      f"main.c/sieve.c/pps/app.c and its CUDA kernels (pps/appcu.cu) built for this GPU",
+                      f"{spec['nmax']}), {dt:.2f} s wall (process start to exit) with -t{threads}; {what}",
             "seconds": dt, "primes": count, "factors": len(lines),
             "identical_to_ours": bool(lines == ours and st.primes == count and st.prime_sum == psum)}
 
@@ -887,6 +895,10 @@ def run_gpu(args) -> None:
                           "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
     cpu = None if args.no_cpu else baseline_sample(args.ref_seconds)
     ref_gpu = None if args.no_cpu else reference_gpu_sample(eng)
+    if ref_gpu is not None and DROPIN_BIN.exists():
+        # the same range through the drop-in: the reference's own CPU sieve and
+        # main loop feeding this library's plugin
+        ref_gpu["dropin"] = reference_gpu_sample(eng, binary=DROPIN_BIN, threads=4)
     mixed_checked, batched = (None, None) if args.no_batched else run_mixed(eng, args.mixed_jobs)
     served, serving = (None, None) if args.no_serving else run_serving(
         window=args.serve_window, long_window=args.serve_long,
