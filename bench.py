@@ -892,7 +892,8 @@ def run_gpu(args) -> None:
                 "sieve": {"bound": "hbm", "achieved": sieve_gbs, "peak": hbm, "unit": "GB/s",
                           "frac": (sieve_gbs / hbm) if (sieve_gbs and hbm) else None,
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                          "work_per_unit": "16 B written per prime (p + Montgomery constant)"}}
+                          "work_per_unit": "16 B written per prime (p + Montgomery constant)",
+                          "p_range_per_s": (args.steps * SPAN / (sieve_ms * 1e-3)) if sieve_ms > 0 else None}}
     cpu = None if args.no_cpu else baseline_sample(args.ref_seconds)
     ref_gpu = None if args.no_cpu else reference_gpu_sample(eng)
     if ref_gpu is not None and DROPIN_BIN.exists():
