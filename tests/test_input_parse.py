@@ -85,3 +85,29 @@ def test_twin_input_reader_matches_oracle(pps, ora):
                       sign=pps.PPS_SIGN_TWIN)
     with pytest.raises(pps.PPSError):
         pps.InputFile(GOLDEN / "inputs" / "twin_newpgen.txt", pmin=5 * 10**10, pmax=6 * 10**10)
+
+
+def test_twin_abcd_reader_edge_cases(pps, ora, tmp_path):
+    """Blank lines between blocks, a block header whose two n differ (the end of
+    the file for the reference's scan, pps/app.c:268-270), and text after the
+    last block: the library's reader and the oracle's agree on every record."""
+    hdr = "ABCD (6*$a+3)*2^{n}+1 & (6*$a+3)*2^{m}-1 [{a}]"
+    body = [hdr.format(n=1000, m=1000, a=2), "3", "5", "", hdr.format(n=1001, m=1001, a=0), "1",
+            "", "", hdr.format(n=1003, m=1003, a=7), "2", "9"]
+    cases = {
+        "blank_lines": body,
+        "mismatched_header_ends": body[:4] + [hdr.format(n=1001, m=1002, a=0), "1"] + body[8:],
+        "trailing_text": body + ["end of file", "4"],
+    }
+    for name, lines in cases.items():
+        path = tmp_path / f"{name}.txt"
+        path.write_text("\n".join(lines) + "\n")
+        spec = dict(pmin=5 * 10**10, pmax=5 * 10**10 + 10**6, sign=pps.PPS_SIGN_TWIN)
+        inp = pps.InputFile(path, **spec)
+        oi = ora.read_input(path, twin=True)
+        info = inp.info()
+        assert info.records == len(oi.records), name
+        assert (info.k0, info.k1) == (6 * oi.k0 + 3, 6 * oi.k1 + 3), name
+        assert (info.n0, info.n1) == (oi.n0, oi.n1), name
+    assert len(ora.read_input(tmp_path / "blank_lines.txt", twin=True).records) == 8
+    assert len(ora.read_input(tmp_path / "mismatched_header_ends.txt", twin=True).records) == 3
